@@ -1,0 +1,145 @@
+// Shared device helpers and host plumbing for the gstools_gb300 kernels.
+//
+// Everything here is written for sm_103a: mbarrier-tracked bulk copies
+// (cp.async.bulk, the TMA engine's untiled form) stage packed mode tables in
+// shared memory, and every wait on an mbarrier is bounded in time so a lost
+// transaction can never hang the GPU -- the kernel records
+// GST_ERR_DEVICE_TIMEOUT in a device error word and returns.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gstools_gb300.h"
+
+#define GST_TRY_CUDA(expr)                                  \
+    do {                                                    \
+        cudaError_t gst_err_ = (expr);                      \
+        if (gst_err_ != cudaSuccess) {                      \
+            ::gst::note_cuda_error(gst_err_);               \
+            return GST_ERR_CUDA;                            \
+        }                                                   \
+    } while (0)
+
+namespace gst {
+
+// ------------------------------------------------------------------ host --
+
+// Remembers the last CUDA error seen by an entry point (for diagnostics).
+void note_cuda_error(cudaError_t err);
+
+// Streaming multiprocessors of the current device (cached per device).
+int sm_count();
+
+// Address of the per-device error word that bounded waits report into.
+unsigned int *device_error_word();
+
+// Current device ordinal, or -1 with GST_ERR_NO_DEVICE semantics.
+int current_device();
+
+// Stream-ordered scratch allocation that always frees on the same stream.
+struct StreamScratch {
+    void *ptr = nullptr;
+    cudaStream_t stream = nullptr;
+    ~StreamScratch() {
+        if (ptr) cudaFreeAsync(ptr, stream);
+    }
+    cudaError_t alloc(size_t bytes, cudaStream_t s) {
+        stream = s;
+        if (bytes == 0) return cudaSuccess;
+        return cudaMallocAsync(&ptr, bytes, s);
+    }
+};
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Device error codes ORed into the error word.
+constexpr unsigned int kErrWaitTimeout = 1u;
+
+// ---------------------------------------------------------------- device --
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar,
+                                                      uint32_t bytes) {
+    asm volatile(
+        "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+            smem_addr(bar)),
+        "r"(bytes)
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_timer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Upper bound on any single wait (nanoseconds).  Every phase a kernel waits
+// for completes within microseconds when the hardware is healthy.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+// Waits for `parity` of `bar`; gives up after kWaitLimitNs, records the
+// timeout in *err and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          unsigned int *err) {
+    if (mbar_test(bar, parity)) return true;
+    const uint64_t t0 = global_timer_ns();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_test(bar, parity)) return true;
+        if ((it & 63u) == 0u) {
+            if (global_timer_ns() - t0 > kWaitLimitNs) {
+                atomicOr(err, kErrWaitTimeout);
+                return false;
+            }
+            __nanosleep(32);
+        }
+    }
+}
+
+// Bulk (TMA) copy global -> shared, completion signalled on `bar` as
+// transaction bytes.  Both addresses 16-byte aligned, bytes % 16 == 0.
+__device__ __forceinline__ void bulk_copy_g2s(void *smem_dst,
+                                              const void *gmem_src,
+                                              uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1], %2, [%3];" ::"r"(smem_addr(smem_dst)),
+        "l"(gmem_src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Round-to-12-significant-bits split used by the mixed-precision kernels:
+// v ~= hi + lo with hi carrying at most 12 significant bits, so the product
+// of two such `hi` values is exact in FP32.
+__device__ __forceinline__ float split_hi12(double v) {
+    const float f = static_cast<float>(v);
+    return __uint_as_float(__float_as_uint(f) & 0xFFFFF000u);
+}
+
+}  // namespace gst

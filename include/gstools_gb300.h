@@ -1,0 +1,180 @@
+/*
+ * gstools_gb300 -- C ABI of the GB300 (sm_103a) randomization-method
+ * summation kernels.
+ *
+ * These entry points replace the native summators that GSTools' generators
+ * call through module-level wrappers:
+ *
+ *   gstools_cython.field.summate          (src/gstools/field/generator.py:22,
+ *                                          wrapper _summate :42-48, called at
+ *                                          RandMeth.__call__ :266-268)
+ *   gstools_cython.field.summate_incompr  (generator.py:24, wrapper
+ *                                          _summate_incompr :51-64, called at
+ *                                          IncomprRandMeth.__call__ :554-560)
+ *   gstools_cython.field.summate_fourier  (generator.py:23, wrapper
+ *                                          _summate_fourier :67-75, called at
+ *                                          Fourier.__call__ :682-689)
+ *
+ * Conventions shared by every entry point
+ * ---------------------------------------
+ * - Arrays are DEVICE pointers (cudaMalloc / torch CUDA memory) of the
+ *   current device, C-contiguous, in the reference's layouts:
+ *   cov_samples (dim, n_modes) row-major, z_1 / z_2 (n_modes,),
+ *   pos (dim, n_pts) row-major, scalar output (n_pts,), vector output
+ *   (dim, n_pts).  Inputs are read-only and borrowed.
+ * - `stream` is a cudaStream_t (NULL = legacy default stream).  Every call is
+ *   asynchronous with respect to the host and ordered on that stream.
+ * - Return value: GST_OK (0) or a GST_ERR_* code; no entry point aborts.
+ *   gst_status_string() names a code.  The `num_threads` argument of the
+ *   reference (CPU thread count) has no counterpart: parallelism is the GPU.
+ * - Internal scratch (packed mode tables, split-mode partial sums, per-axis
+ *   phase tables) is taken from the stream-ordered allocator
+ *   (cudaMallocAsync) and released on the same stream.
+ * - Results are the raw mode sums of the reference; the caller applies
+ *   sqrt(var / N) and the nugget exactly as generator.py:269-270 and
+ *   :561-567 do.  The grid entry points take an optional `scale` that is
+ *   fused into the epilogue (pass 1.0 for raw sums).
+ */
+#ifndef GSTOOLS_GB300_H
+#define GSTOOLS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GST_OK 0
+#define GST_ERR_INVALID_ARGUMENT 1 /* bad size, NULL pointer, ... */
+#define GST_ERR_UNSUPPORTED_DIM 2  /* dim outside the supported range */
+#define GST_ERR_CUDA 3             /* a CUDA runtime call failed */
+#define GST_ERR_ALIGNMENT 4        /* a pointer violates the stated alignment */
+#define GST_ERR_NO_DEVICE 5        /* no usable sm_103 device is current */
+#define GST_ERR_DEVICE_TIMEOUT 6   /* a bounded device-side wait gave up */
+#define GST_ERR_TOO_LARGE 7        /* a size exceeds a documented maximum */
+
+/* Output element types for the mixed-precision and grid entry points. */
+#define GST_OUT_F64 0
+#define GST_OUT_F32 1
+
+/* Library version as 10000*major + 100*minor + patch. */
+int gst_version(void);
+
+/* Human-readable name of a status code (static storage). */
+const char *gst_status_string(int status);
+
+/* cudaError_t value behind the calling thread's last GST_ERR_CUDA. */
+int gst_last_cuda_error(void);
+
+/* Reads and clears the device-side error word that bounded waits in the
+ * kernels set when they give up (GST_ERR_DEVICE_TIMEOUT bits).  Synchronises
+ * `stream`.  *device_error receives the word (0 = none). */
+int gst_read_device_error(void *stream, uint32_t *device_error);
+
+/* ----------------------------------------------------------------------- */
+/* Plain FP64 pointwise kernels (parity anchors).                           */
+/* ----------------------------------------------------------------------- */
+
+/* summate: out[i] = sum_j z_1[j] cos(<k_j, x_i>) + z_2[j] sin(<k_j, x_i>).
+ * Replaces gstools_cython.field.summate (generator.py:22, math :193-199).
+ * dim in 1..4.  FP64 throughout. */
+int gst_summate_f64(int dim, int64_t n_modes, int64_t n_pts,
+                    const double *cov_samples, const double *z_1,
+                    const double *z_2, const double *pos, double *out,
+                    void *stream);
+
+/* summate_incompr: out[c, i] = sum_j (delta_c0 - k_cj k_0j / |k_j|^2)
+ *                    (z_1[j] cos(<k_j, x_i>) + z_2[j] sin(<k_j, x_i>)).
+ * Replaces gstools_cython.field.summate_incompr (generator.py:24, math
+ * :479-495).  dim in 2..3.  out is (dim, n_pts).  FP64 throughout. */
+int gst_summate_incompr_f64(int dim, int64_t n_modes, int64_t n_pts,
+                            const double *cov_samples, const double *z_1,
+                            const double *z_2, const double *pos, double *out,
+                            void *stream);
+
+/* summate_fourier: out[i] = sum_j f[j] (z_1[j] cos(<k_j, x_i>)
+ *                                       + z_2[j] sin(<k_j, x_i>)).
+ * Replaces gstools_cython.field.summate_fourier (generator.py:23, called at
+ * :682-689).  `modes` is (dim, n_modes) like cov_samples.  dim in 1..4. */
+int gst_summate_fourier_f64(int dim, int64_t n_modes, int64_t n_pts,
+                            const double *spectrum_factor, const double *modes,
+                            const double *z_1, const double *z_2,
+                            const double *pos, double *out, void *stream);
+
+/* ----------------------------------------------------------------------- */
+/* Mixed-precision pointwise kernels (same inputs, FP64 in).                */
+/* The phase is reduced to turns exactly (error-free FP32 splitting of the  */
+/* FP64 wave vectors and positions), sin/cos run on the SFU in FP32, each   */
+/* 256-mode block is summed in FP32 and blocks are accumulated in FP64.     */
+/* Domain: |k_d x_d| / (2 pi) < 2^21 turns per axis.                        */
+/* ----------------------------------------------------------------------- */
+
+/* Same contract as gst_summate_f64; `out` is double (GST_OUT_F64) or float
+ * (GST_OUT_F32).  dim in 1..3. */
+int gst_summate_mixed(int dim, int64_t n_modes, int64_t n_pts,
+                      const double *cov_samples, const double *z_1,
+                      const double *z_2, const double *pos, void *out,
+                      int out_type, void *stream);
+
+/* Same contract as gst_summate_incompr_f64, mixed precision.  dim in 2..3. */
+int gst_summate_incompr_mixed(int dim, int64_t n_modes, int64_t n_pts,
+                              const double *cov_samples, const double *z_1,
+                              const double *z_2, const double *pos, void *out,
+                              int out_type, void *stream);
+
+/* ----------------------------------------------------------------------- */
+/* Structured grids.                                                        */
+/* A structured grid is the meshgrid ("ij" order, last axis fastest) of     */
+/* `dim` axis arrays (generate_grid, src/gstools/tools/geometric.py:340-356) */
+/* passed concatenated in `axes` (axis_len[0] + ... + axis_len[dim-1]       */
+/* values; `axes` is device memory, `axis_len` is HOST memory).             */
+/* The reference isometrizes the materialised grid with a linear  */
+/* map M (covmodel/base.py:572-582); because <k, M x> = <M^T k, x>, callers */
+/* pass cov_samples already multiplied by M^T and the kernels never         */
+/* materialise the grid.  Output shape is (axis_len[0], ..., axis_len[d-1]) */
+/* (scalar) or (dim, axis_len[0], ...) (vector).                            */
+/* ----------------------------------------------------------------------- */
+
+/* Plain FP64 pointwise kernel over structured-grid points. dim in 1..4. */
+int gst_summate_grid_f64(int dim, int64_t n_modes, const int64_t *axis_len,
+                         const double *axes, const double *cov_samples,
+                         const double *z_1, const double *z_2, double *out,
+                         void *stream);
+
+/* Mixed-precision pointwise kernel over structured-grid points.  dim 1..3.
+ * `scale` multiplies the result (1.0 = raw sums). */
+int gst_summate_grid_mixed(int dim, int64_t n_modes, const int64_t *axis_len,
+                           const double *axes, const double *cov_samples,
+                           const double *z_1, const double *z_2, void *out,
+                           int out_type, double scale, void *stream);
+
+/* FP64 incompressible field over structured-grid points. dim in 2..3. */
+int gst_summate_incompr_grid_f64(int dim, int64_t n_modes,
+                                 const int64_t *axis_len, const double *axes,
+                                 const double *cov_samples, const double *z_1,
+                                 const double *z_2, double *out, void *stream);
+
+/* Mixed-precision incompressible field over structured-grid points. */
+int gst_summate_incompr_grid_mixed(int dim, int64_t n_modes,
+                                   const int64_t *axis_len, const double *axes,
+                                   const double *cov_samples,
+                                   const double *z_1, const double *z_2,
+                                   void *out, int out_type, double scale,
+                                   void *stream);
+
+/* ----------------------------------------------------------------------- */
+/* Diagnostics (no reference counterpart).                                  */
+/* ----------------------------------------------------------------------- */
+
+/* Launches one throughput probe on `stream`: kind 0 = FP32 FMA, 1 = FP64
+ * FMA, 2 = SFU sin.approx.  *ops_per_launch receives the operations the
+ * launch executes (an FMA counts 2 flops, a sin 1 op); the caller times the
+ * launch.  `sink` is a device buffer of >= 256 floats. */
+int gst_peak_probe(int kind, int64_t iters, float *sink,
+                   double *ops_per_launch, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSTOOLS_GB300_H */

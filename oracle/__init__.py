@@ -1,0 +1,29 @@
+"""FP64 CPU oracle for the randomization-method summation.
+
+TEST INFRASTRUCTURE ONLY.  This package is the checker: tests/, the smoke
+check in __graft_entry__ and the CPU-baseline leg of bench.py import it.  The
+gstools_gb300 product never imports it, and the product path has no CPU
+fallback that could route here.
+
+Two independent restatements of the reference formulas
+(src/gstools/field/generator.py:193-199 for ``summate``, :479-495 for
+``summate_incompr``, :682-689 for ``summate_fourier``):
+
+* ``c_summate`` / ``c_summate_incompr`` / ``c_summate_fourier``: the C/OpenMP
+  library built from ``summate_oracle.c`` (the primary oracle and the timed CPU
+  baseline);
+* ``np_summate`` / ``np_summate_incompr`` / ``np_summate_fourier``: a chunked
+  numpy witness used to cross-check the C oracle.
+"""
+
+from .oracle import (  # noqa: F401
+    build,
+    c_summate,
+    c_summate_fourier,
+    c_summate_incompr,
+    library_path,
+    num_threads,
+    np_summate,
+    np_summate_fourier,
+    np_summate_incompr,
+)

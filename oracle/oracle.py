@@ -1,0 +1,177 @@
+"""Loader for the C oracle and the numpy witness (test infrastructure only).
+
+Every function here restates the reference's formulas:
+
+* summate          -- src/gstools/field/generator.py:193-199
+* summate_incompr  -- src/gstools/field/generator.py:479-495
+* summate_fourier  -- src/gstools/field/generator.py:682-689
+
+Inputs follow the reference's array layouts: ``cov_samples`` (dim, N),
+``z_1``/``z_2`` (N,), ``pos`` (dim, n), all float64.
+"""
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_NAME = "liboracle_summate.so"
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path():
+    """Path of the compiled C oracle."""
+    return os.path.join(_HERE, _LIB_NAME)
+
+
+def build(force=False):
+    """Compile the C oracle with its Makefile (gcc, OpenMP)."""
+    src = os.path.join(_HERE, "summate_oracle.c")
+    out = library_path()
+    if (
+        not force
+        and os.path.exists(out)
+        and os.path.getmtime(out) >= os.path.getmtime(src)
+    ):
+        return out
+    subprocess.run(["make", "-s", "-C", _HERE, "-B"], check=True)
+    return out
+
+
+def _load():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            lib = ctypes.CDLL(library_path())
+            dp = ctypes.POINTER(ctypes.c_double)
+            i64 = ctypes.c_int64
+            for name in ("oracle_summate", "oracle_summate_incompr"):
+                fn = getattr(lib, name)
+                fn.restype = ctypes.c_int
+                fn.argtypes = [ctypes.c_int, i64, i64, dp, dp, dp, dp, dp,
+                               ctypes.c_int]
+            fn = lib.oracle_summate_fourier
+            fn.restype = ctypes.c_int
+            fn.argtypes = [ctypes.c_int, i64, i64, dp, dp, dp, dp, dp, dp,
+                           ctypes.c_int]
+            lib.oracle_num_threads.restype = ctypes.c_int
+            lib.oracle_num_threads.argtypes = []
+            _lib = lib
+    return _lib
+
+
+def num_threads():
+    """OpenMP threads the C oracle uses by default."""
+    return _load().oracle_num_threads()
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _check(cov, z_1, z_2, pos):
+    cov, z_1, z_2, pos = _f64(cov), _f64(z_1), _f64(z_2), _f64(pos)
+    cov = np.atleast_2d(cov)
+    pos = pos.reshape(cov.shape[0], -1)
+    if z_1.shape != (cov.shape[1],) or z_2.shape != (cov.shape[1],):
+        raise ValueError("oracle: z_1/z_2 must have shape (N,)")
+    return cov, z_1, z_2, pos
+
+
+def c_summate(cov_samples, z_1, z_2, pos, num_threads=0):
+    """C oracle of ``summate`` (generator.py:193-199)."""
+    cov, z_1, z_2, pos = _check(cov_samples, z_1, z_2, pos)
+    dim, n_modes = cov.shape
+    n_pts = pos.shape[1]
+    out = np.empty(n_pts, dtype=np.float64)
+    rc = _load().oracle_summate(dim, n_modes, n_pts, _ptr(cov), _ptr(z_1),
+                                _ptr(z_2), _ptr(pos), _ptr(out),
+                                int(num_threads or 0))
+    if rc:
+        raise ValueError(f"oracle_summate failed with code {rc}")
+    return out
+
+
+def c_summate_incompr(cov_samples, z_1, z_2, pos, num_threads=0):
+    """C oracle of ``summate_incompr`` (generator.py:479-495)."""
+    cov, z_1, z_2, pos = _check(cov_samples, z_1, z_2, pos)
+    dim, n_modes = cov.shape
+    n_pts = pos.shape[1]
+    out = np.empty((dim, n_pts), dtype=np.float64)
+    rc = _load().oracle_summate_incompr(dim, n_modes, n_pts, _ptr(cov),
+                                        _ptr(z_1), _ptr(z_2), _ptr(pos),
+                                        _ptr(out), int(num_threads or 0))
+    if rc:
+        raise ValueError(f"oracle_summate_incompr failed with code {rc}")
+    return out
+
+
+def c_summate_fourier(spectrum_factor, modes, z_1, z_2, pos, num_threads=0):
+    """C oracle of ``summate_fourier`` (generator.py:682-689)."""
+    modes, z_1, z_2, pos = _check(modes, z_1, z_2, pos)
+    fac = _f64(spectrum_factor)
+    dim, n_modes = modes.shape
+    n_pts = pos.shape[1]
+    out = np.empty(n_pts, dtype=np.float64)
+    rc = _load().oracle_summate_fourier(dim, n_modes, n_pts, _ptr(fac),
+                                        _ptr(modes), _ptr(z_1), _ptr(z_2),
+                                        _ptr(pos), _ptr(out),
+                                        int(num_threads or 0))
+    if rc:
+        raise ValueError(f"oracle_summate_fourier failed with code {rc}")
+    return out
+
+
+def _phase_chunks(cov, pos, chunk):
+    for start in range(0, pos.shape[1], chunk):
+        stop = min(start + chunk, pos.shape[1])
+        # phase[j, i] = sum_d k[d, j] x[d, i], accumulated over d in order
+        phase = np.zeros((cov.shape[1], stop - start))
+        for d in range(cov.shape[0]):
+            phase += np.outer(cov[d], pos[d, start:stop])
+        yield start, stop, phase
+
+
+def np_summate(cov_samples, z_1, z_2, pos, chunk=4096):
+    """numpy witness of ``summate`` (generator.py:193-199)."""
+    cov, z_1, z_2, pos = _check(cov_samples, z_1, z_2, pos)
+    out = np.empty(pos.shape[1])
+    for start, stop, phase in _phase_chunks(cov, pos, chunk):
+        out[start:stop] = z_1 @ np.cos(phase) + z_2 @ np.sin(phase)
+    return out
+
+
+def np_summate_incompr(cov_samples, z_1, z_2, pos, chunk=4096):
+    """numpy witness of ``summate_incompr`` (generator.py:479-495)."""
+    cov, z_1, z_2, pos = _check(cov_samples, z_1, z_2, pos)
+    dim = cov.shape[0]
+    k2 = np.sum(cov**2, axis=0)
+    e1 = np.zeros(dim)
+    e1[0] = 1.0
+    proj = e1[:, None] - cov * cov[0] / k2  # (dim, N)
+    out = np.empty((dim, pos.shape[1]))
+    for start, stop, phase in _phase_chunks(cov, pos, chunk):
+        amp = z_1[:, None] * np.cos(phase) + z_2[:, None] * np.sin(phase)
+        out[:, start:stop] = proj @ amp
+    return out
+
+
+def np_summate_fourier(spectrum_factor, modes, z_1, z_2, pos, chunk=4096):
+    """numpy witness of ``summate_fourier`` (generator.py:682-689)."""
+    modes, z_1, z_2, pos = _check(modes, z_1, z_2, pos)
+    fac = _f64(spectrum_factor)
+    out = np.empty(pos.shape[1])
+    for start, stop, phase in _phase_chunks(modes, pos, chunk):
+        out[start:stop] = (fac * z_1) @ np.cos(phase) + (fac * z_2) @ np.sin(
+            phase
+        )
+    return out

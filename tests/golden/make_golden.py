@@ -1,0 +1,260 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Run from the repository root, where the reference tree is available:
+
+    python tests/golden/make_golden.py
+
+The reference's Python package (RNG, covariance models, RandMeth,
+IncomprRandMeth, SRF) is imported with ``reference_import`` and drives the
+FP64 C oracle in place of the absent ``gstools_cython.field`` kernels.  Before
+anything is written, every literal golden value that the reference's own tests
+assert on this path is reproduced here (``assertAlmostEqual``'s 7 places):
+
+* tests/test_randmeth.py:35-36, 40-41, 50-51, 55-56, 60-61, 70-71
+* tests/test_incomprrandmeth.py:36-38, 58-59
+* tests/test_srf.py:269-275
+* tests/test_rng.py:22-37
+
+The 3-D RandMeth goldens (test_randmeth.py:45-46, 65-66;
+test_incomprrandmeth.py:42-44) need emcee's MCMC sampler, which is absent, so
+they cannot be reproduced and are not used.
+
+The workload inputs (cov_samples, z_1, z_2) for the benchmark shapes are drawn
+by the reference's own RNG: through the closed-form inversion path where the
+model has a ppf (2-D Gaussian), and through ``sampling="inversion"`` (scipy's
+numerical ppf of the reference's radial cdf) for the 3-D models.
+
+Outputs: ``reference_goldens.npz`` (tiny cases with their literal goldens) and
+``workloads.npz`` (mode sets and oracle outputs on sub-samples of the
+benchmark point sets).
+"""
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+import oracle  # noqa: E402
+from reference_import import import_gstools  # noqa: E402
+
+PLACES = 7
+
+
+def check(value, expected, what):
+    if round(abs(value - expected), PLACES) != 0:
+        raise AssertionError(f"{what}: got {value!r}, reference {expected!r}")
+
+
+def modes_of(gen):
+    return {
+        "cov": np.array(gen._cov_sample, dtype=np.float64),
+        "z1": np.array(gen._z_1, dtype=np.float64),
+        "z2": np.array(gen._z_2, dtype=np.float64),
+    }
+
+
+def reference_goldens(gs):
+    from gstools.field.generator import IncomprRandMeth, RandMeth
+    from gstools.random.rng import RNG
+
+    out = {}
+
+    def store(name, gen, pos, field, expected, idx, var):
+        m = modes_of(gen)
+        pos = np.atleast_2d(np.asarray(pos, dtype=np.float64))
+        for key, val in m.items():
+            out[f"{name}/{key}"] = val
+        out[f"{name}/pos"] = pos
+        out[f"{name}/field"] = np.asarray(field)
+        out[f"{name}/expected"] = np.asarray(expected, dtype=np.float64)
+        out[f"{name}/index"] = np.asarray(idx, dtype=np.int64)
+        out[f"{name}/var"] = np.float64(var)
+        out[f"{name}/seed"] = np.int64(gen.seed)
+        for e, i in zip(expected, idx):
+            check(np.asarray(field)[tuple(i)], e, f"{name}{tuple(i)}")
+
+    # tests/test_randmeth.py:15-71
+    cm1 = gs.Gaussian(dim=1, var=1.5, len_scale=3.5)
+    cm2 = gs.Gaussian(dim=2, var=1.5, len_scale=3.5)
+    seed = 19031977
+    x_t = np.linspace(0.0, 10.0, 10)
+    y_t = np.linspace(-5.0, 5.0, 10)
+    rm1 = RandMeth(cm1, mode_no=100, seed=seed)
+    store("randmeth_1d", rm1, (x_t,), rm1((x_t,)),
+          [3.19799030, 2.44848295], [[0], [1]], 1.5)
+    rm2 = RandMeth(cm2, mode_no=100, seed=seed)
+    store("randmeth_2d", rm2, (x_t, y_t), rm2((x_t, y_t)),
+          [1.67318010, 2.12310269], [[0], [1]], 1.5)
+    rm2.seed = 74893621
+    store("randmeth_2d_reseed", rm2, (x_t, y_t), rm2((x_t, y_t)),
+          [-1.94278053, -1.12401651], [[0], [1]], 1.5)
+    rm2.mode_no = 800
+    store("randmeth_2d_800", rm2, (x_t, y_t), rm2((x_t, y_t)),
+          [-3.20809251, -2.62032778], [[0], [1]], 1.5)
+
+    # tests/test_incomprrandmeth.py:17-38
+    ci2 = gs.Gaussian(dim=2, var=1.5, len_scale=2.5)
+    ir2 = IncomprRandMeth(ci2, mode_no=100, seed=seed)
+    store("incompr_2d", ir2, (x_t, y_t), ir2((x_t, y_t)),
+          [0.50751115, 1.03291018, -0.22003005],
+          [[0, 0], [0, 1], [1, 1]], 1.5)
+
+    # tests/test_incomprrandmeth.py:50-59: VectorField mean (structured)
+    x_g = np.linspace(0.0, 10.0, 9)
+    y_g = np.linspace(-5.0, 5.0, 16)
+    srf = gs.SRF(ci2, mean=(0.5, 0), generator="VectorField", seed=198412031)
+    fld = srf.structured((x_g, y_g))
+    means = [np.mean(fld[0]), np.mean(fld[1])]
+    check(means[0], 1.3025621393180298, "vector_mean[0]")
+    check(means[1], -0.04729596839446052, "vector_mean[1]")
+    m = modes_of(srf.generator)
+    for key, val in m.items():
+        out[f"vector_mean/{key}"] = val
+    out["vector_mean/x"] = x_g
+    out["vector_mean/y"] = y_g
+    out["vector_mean/var"] = np.float64(1.5)
+    out["vector_mean/mean_u"] = np.float64(srf.generator.mean_u)
+    out["vector_mean/mean"] = np.array([0.5, 0.0])
+    out["vector_mean/expected"] = np.array(
+        [1.3025621393180298, -0.04729596839446052])
+
+    # tests/test_srf.py:259-275: IncomprRandMeth through SRF, mean 0.3
+    rng = np.random.RandomState(123018)
+    xs = rng.uniform(0.0, 10, 100)
+    ys = rng.uniform(0.0, 10, 100)
+    cm = gs.Gaussian(dim=2, var=0.5, len_scale=1.0)
+    srf = gs.SRF(cm, mean=0.3, mode_no=100, generator="IncomprRandMeth",
+                 mean_velocity=0.5)
+    fld = srf((xs, ys), seed=476356)
+    check(fld[0, 0], 1.23693272, "srf_incompr_unstruct[0,0]")
+    check(fld[0, 1], 0.89242284, "srf_incompr_unstruct[0,1]")
+    m = modes_of(srf.generator)
+    for key, val in m.items():
+        out[f"srf_incompr_unstruct/{key}"] = val
+    out["srf_incompr_unstruct/pos"] = np.array([xs, ys])
+    out["srf_incompr_unstruct/expected"] = np.array([1.23693272, 0.89242284])
+    out["srf_incompr_unstruct/index"] = np.array([[0, 0], [0, 1]])
+    out["srf_incompr_unstruct/field"] = fld
+    x_g = np.linspace(0.0, 12.0, 48)
+    y_g = np.linspace(0.0, 10.0, 46)
+    fld = srf((x_g, y_g), seed=4734654, mesh_type="structured")
+    check(fld[0, 0, 0], 1.07812013, "srf_incompr_struct[0,0,0]")
+    check(fld[0, 1, 0], 1.06180674, "srf_incompr_struct[0,1,0]")
+    m = modes_of(srf.generator)
+    for key, val in m.items():
+        out[f"srf_incompr_struct/{key}"] = val
+    out["srf_incompr_struct/x"] = x_g
+    out["srf_incompr_struct/y"] = y_g
+    out["srf_incompr_struct/expected"] = np.array([1.07812013, 1.06180674])
+    out["srf_incompr_struct/index"] = np.array([[0, 0, 0], [0, 1, 0]])
+    out["srf_incompr_struct/field"] = fld
+
+    # tests/test_rng.py:20-37: normal streams of RNG(19031977)
+    rng = RNG(seed)
+    z1 = rng.random.normal(size=100)
+    z2 = rng.random.normal(size=100)
+    for v, e, w in ((z1[0], -1.93013270, "z1[0]"), (z1[1], 0.46330478, "z1[1]"),
+                    (z2[0], -0.25536086, "z2[0]"), (z2[1], 0.98298696, "z2[1]")):
+        check(v, e, w)
+    out["rng_normal/z1"] = z1
+    out["rng_normal/z2"] = z2
+    return out
+
+
+def workloads(gs):
+    from gstools.field.generator import IncomprRandMeth, RandMeth
+    from gstools.tools.geometric import generate_grid, matrix_isometrize
+
+    out = {}
+    seed = 20170519
+
+    # 2-D Gaussian, var 1, len_scale 10, 1000 modes, 100 000 points in
+    # [0, 100]^2 drawn by RandomState(20170519); oracle on the first 4096.
+    model = gs.Gaussian(dim=2, var=1.0, len_scale=10.0)
+    gen = RandMeth(model, mode_no=1000, seed=seed)
+    pos = np.random.RandomState(seed).uniform(0.0, 100.0, (2, 100_000))
+    for key, val in modes_of(gen).items():
+        out[f"gau2d/{key}"] = val
+    sub = pos[:, :4096]
+    out["gau2d/pos_head"] = sub
+    out["gau2d/summed_head"] = oracle.c_summate(gen._cov_sample, gen._z_1,
+                                               gen._z_2, sub)
+
+    # 3-D Exponential, var 2, len_scale [20, 10, 5], 2000 modes; structured
+    # grid 0..255 per axis (unit spacing).  Modes by scipy inversion.
+    model = gs.Exponential(dim=3, var=2.0, len_scale=[20.0, 10.0, 5.0])
+    gen = RandMeth(model, mode_no=2000, seed=seed, sampling="inversion")
+    for key, val in modes_of(gen).items():
+        out[f"exp3d/{key}"] = val
+    iso = matrix_isometrize(3, model.angles, model.anis)
+    out["exp3d/isometrize"] = iso
+    axes = [np.arange(0.0, 256.0, 17.0), np.arange(3.0, 256.0, 23.0),
+            np.arange(1.0, 256.0, 11.0)]
+    grid = model.isometrize(generate_grid(axes))
+    out["exp3d/sub_x"], out["exp3d/sub_y"], out["exp3d/sub_z"] = axes
+    out["exp3d/summed_sub"] = oracle.c_summate(gen._cov_sample, gen._z_1,
+                                              gen._z_2, grid)
+
+    # 3-D Gaussian incompressible, var 1, len_scale 8, 2000 modes, mean
+    # velocity 1.0 on a 192^3 unit grid.  Modes by scipy inversion.
+    model = gs.Gaussian(dim=3, var=1.0, len_scale=8.0)
+    gen = IncomprRandMeth(model, mode_no=2000, seed=seed,
+                          sampling="inversion", mean_velocity=1.0)
+    for key, val in modes_of(gen).items():
+        out[f"incompr3d/{key}"] = val
+    axes = [np.arange(0.0, 192.0, 13.0), np.arange(5.0, 192.0, 19.0),
+            np.arange(2.0, 192.0, 7.0)]
+    grid = model.isometrize(generate_grid(axes))
+    out["incompr3d/sub_x"], out["incompr3d/sub_y"], out["incompr3d/sub_z"] = (
+        axes)
+    out["incompr3d/summed_sub"] = oracle.c_summate_incompr(
+        gen._cov_sample, gen._z_1, gen._z_2, grid)
+
+    # 3-D Gaussian for the differentiable case: var 1, len_scale 16,
+    # anisotropy [0.8, 0.6], angles [0.3, 0.2, 0.1], 4000 modes.
+    model = gs.Gaussian(dim=3, var=1.0, len_scale=16.0, anis=[0.8, 0.6],
+                        angles=[0.3, 0.2, 0.1])
+    gen = RandMeth(model, mode_no=4000, seed=seed, sampling="inversion")
+    for key, val in modes_of(gen).items():
+        out[f"gau3d_grad/{key}"] = val
+    out["gau3d_grad/isometrize"] = matrix_isometrize(3, model.angles,
+                                                     model.anis)
+    pts = np.random.RandomState(seed + 1).uniform(0.0, 128.0, (3, 2048))
+    out["gau3d_grad/pos"] = pts
+    out["gau3d_grad/summed"] = oracle.c_summate(
+        gen._cov_sample, gen._z_1, gen._z_2, model.isometrize(pts))
+
+    # Radial spectral densities (pdf/cdf) the host-side samplers must follow.
+    r = np.geomspace(1e-3, 10.0, 64)
+    for name, mdl in (
+        ("gau3", gs.Gaussian(dim=3, len_scale=8.0)),
+        ("exp3", gs.Exponential(dim=3, len_scale=20.0)),
+        ("exp2", gs.Exponential(dim=2, len_scale=20.0)),
+        ("gau2", gs.Gaussian(dim=2, len_scale=10.0)),
+        ("mat2", gs.Matern(dim=2, nu=1.5, len_scale=10.0)),
+        ("mat3", gs.Matern(dim=3, nu=1.5, len_scale=10.0)),
+    ):
+        out[f"spectral/{name}/r"] = r
+        out[f"spectral/{name}/pdf"] = mdl.spectral_rad_pdf(r)
+        if mdl.has_cdf:
+            out[f"spectral/{name}/cdf"] = mdl.spectral_rad_cdf(r)
+        out[f"spectral/{name}/len_rescaled"] = np.float64(mdl.len_rescaled)
+    return out
+
+
+def main():
+    gs = import_gstools()
+    golden = reference_goldens(gs)
+    np.savez_compressed(os.path.join(HERE, "reference_goldens.npz"), **golden)
+    work = workloads(gs)
+    np.savez_compressed(os.path.join(HERE, "workloads.npz"), **work)
+    print(f"wrote {len(golden)} + {len(work)} arrays to {HERE}")
+
+
+if __name__ == "__main__":
+    main()

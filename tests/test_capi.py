@@ -1,0 +1,54 @@
+"""The C-ABI library: it loads and exports every entry point the header
+declares.  Only non-compute calls are made here (no GPU needed)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from gstools_gb300 import _native, build
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(__file__)), "include",
+                      "gstools_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gst_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _native.load()
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for required in ("gst_summate_f64", "gst_summate_incompr_f64",
+                     "gst_summate_mixed", "gst_summate_grid_f64"):
+        assert required in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_binding_table_matches_header():
+    assert set(declared_functions()) == set(_native.SIGNATURES)
+
+
+def test_version_and_status_strings(lib):
+    assert lib.gst_version() >= 100
+    assert _native.status_string(0) == "ok"
+    assert "argument" in _native.status_string(_native.GST_ERR_INVALID_ARGUMENT)
+    assert _native.status_string(12345) == "unknown status"
+
+
+def test_library_is_the_in_tree_build(lib):
+    assert os.path.dirname(_native.library_path()) == os.path.dirname(
+        os.path.abspath(_native.__file__))
+    assert isinstance(lib, ctypes.CDLL)

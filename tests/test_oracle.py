@@ -1,0 +1,144 @@
+"""The FP64 oracle, pinned against the reference's own golden values.
+
+Each case in reference_goldens.npz carries the inputs the reference's RNG drew
+(cov_samples, z_1, z_2), the positions, and the literal values the reference's
+tests assert (tests/test_randmeth.py, tests/test_incomprrandmeth.py,
+tests/test_srf.py).  The C oracle and the numpy witness must reproduce them to
+the reference tests' 7 decimal places, and agree with each other to ~1e-14.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+
+PLACES = 7
+
+
+def assert_places(value, expected, places=PLACES):
+    assert round(abs(float(value) - float(expected)), places) == 0, (
+        value, expected)
+
+
+RANDMETH_CASES = ["randmeth_1d", "randmeth_2d", "randmeth_2d_reseed",
+                  "randmeth_2d_800"]
+
+
+@pytest.mark.parametrize("name", RANDMETH_CASES)
+def test_randmeth_goldens(ref_goldens, name):
+    # tests/test_randmeth.py:35-71 (1-D, 2-D, reseed 74893621, mode_no 800)
+    c = ref_goldens.case(name)
+    n_modes = c["cov"].shape[1]
+    for fn in (oracle.c_summate, oracle.np_summate):
+        summed = fn(c["cov"], c["z1"], c["z2"], c["pos"])
+        field = np.sqrt(c["var"] / n_modes) * summed
+        for exp, idx in zip(c["expected"], c["index"]):
+            assert_places(field[tuple(idx)], exp)
+        np.testing.assert_allclose(field, c["field"], rtol=0, atol=1e-13)
+
+
+def test_incompr_golden(ref_goldens):
+    # tests/test_incomprrandmeth.py:34-38 (mean_velocity 1)
+    c = ref_goldens.case("incompr_2d")
+    n_modes = c["cov"].shape[1]
+    for fn in (oracle.c_summate_incompr, oracle.np_summate_incompr):
+        summed = fn(c["cov"], c["z1"], c["z2"], c["pos"])
+        e1 = np.array([[1.0], [0.0]])
+        field = e1 + np.sqrt(c["var"] / n_modes) * summed
+        for exp, idx in zip(c["expected"], c["index"]):
+            assert_places(field[tuple(idx)], exp)
+
+
+def test_vector_mean_golden(ref_goldens):
+    # tests/test_incomprrandmeth.py:50-59 (VectorField, structured, mean 0.5)
+    c = ref_goldens.case("vector_mean")
+    n_modes = c["cov"].shape[1]
+    grid = np.array(np.meshgrid(c["x"], c["y"], indexing="ij")).reshape(2, -1)
+    summed = oracle.c_summate_incompr(c["cov"], c["z1"], c["z2"], grid)
+    field = (c["mean_u"] * np.array([[1.0], [0.0]])
+             + c["mean_u"] * np.sqrt(c["var"] / n_modes) * summed
+             + c["mean"][:, None])
+    assert_places(np.mean(field[0]), c["expected"][0])
+    assert_places(np.mean(field[1]), c["expected"][1])
+
+
+def test_srf_incompr_goldens(ref_goldens):
+    # tests/test_srf.py:259-275 (IncomprRandMeth via SRF, mean 0.3, u 0.5)
+    var, mean_u, mean = 0.5, 0.5, 0.3
+    c = ref_goldens.case("srf_incompr_unstruct")
+    n_modes = c["cov"].shape[1]
+    summed = oracle.c_summate_incompr(c["cov"], c["z1"], c["z2"], c["pos"])
+    field = (mean_u * np.array([[1.0], [0.0]])
+             + mean_u * np.sqrt(var / n_modes) * summed + mean)
+    for exp, idx in zip(c["expected"], c["index"]):
+        assert_places(field[tuple(idx)], exp)
+    c = ref_goldens.case("srf_incompr_struct")
+    grid = np.array(np.meshgrid(c["x"], c["y"], indexing="ij")).reshape(2, -1)
+    summed = oracle.c_summate_incompr(c["cov"], c["z1"], c["z2"], grid)
+    field = (mean_u * np.array([[1.0], [0.0]])
+             + mean_u * np.sqrt(var / n_modes) * summed + mean)
+    field = field.reshape((2, len(c["x"]), len(c["y"])))
+    for exp, idx in zip(c["expected"], c["index"]):
+        assert_places(field[tuple(idx)], exp)
+
+
+@pytest.mark.parametrize("name,fn", [
+    ("exp3d", "summed_sub"), ("gau2d", "summed_head")])
+def test_workload_oracle_outputs(workloads, name, fn):
+    c = workloads.case(name)
+    if name == "gau2d":
+        pos = c["pos_head"]
+    else:
+        grid = np.array(np.meshgrid(c["sub_x"], c["sub_y"], c["sub_z"],
+                                    indexing="ij")).reshape(3, -1)
+        pos = c["isometrize"] @ grid
+    got = oracle.c_summate(c["cov"], c["z1"], c["z2"], pos)
+    np.testing.assert_array_equal(got, c[fn])
+    wit = oracle.np_summate(c["cov"], c["z1"], c["z2"], pos)
+    assert np.max(np.abs(wit - got)) <= 1e-12 * np.max(np.abs(got))
+
+
+def test_c_and_numpy_agree_random():
+    rng = np.random.RandomState(7)
+    for dim in (1, 2, 3, 4):
+        cov = rng.normal(size=(dim, 37)) * 0.3
+        z1, z2 = rng.normal(size=37), rng.normal(size=37)
+        pos = rng.uniform(-50, 50, size=(dim, 301))
+        a = oracle.c_summate(cov, z1, z2, pos)
+        b = oracle.np_summate(cov, z1, z2, pos)
+        assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(a))
+        if dim in (2, 3):
+            a = oracle.c_summate_incompr(cov, z1, z2, pos)
+            b = oracle.np_summate_incompr(cov, z1, z2, pos)
+            assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(a))
+        f = rng.uniform(0.1, 1.0, size=37)
+        a = oracle.c_summate_fourier(f, cov, z1, z2, pos)
+        b = oracle.np_summate_fourier(f, cov, z1, z2, pos)
+        assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(a))
+
+
+def test_oracle_empty_inputs():
+    cov = np.zeros((2, 0))
+    out = oracle.c_summate(cov, np.zeros(0), np.zeros(0), np.ones((2, 5)))
+    np.testing.assert_array_equal(out, np.zeros(5))
+    out = oracle.c_summate(np.ones((2, 3)), np.ones(3), np.ones(3),
+                           np.zeros((2, 0)))
+    assert out.shape == (0,)
+
+
+def test_oracle_rejects_bad_shapes():
+    with pytest.raises(ValueError):
+        oracle.c_summate(np.ones((2, 3)), np.ones(2), np.ones(3),
+                         np.ones((2, 4)))
+
+
+def test_oracle_planted_error_is_caught(ref_goldens):
+    """A mistake planted in the oracle's inputs must break the golden check."""
+    c = ref_goldens.case("randmeth_2d")
+    z2 = c["z2"].copy()
+    z2[0] += 1e-3
+    summed = oracle.c_summate(c["cov"], c["z1"], z2, c["pos"])
+    field = np.sqrt(c["var"] / c["cov"].shape[1]) * summed
+    with pytest.raises(AssertionError):
+        for exp, idx in zip(c["expected"], c["index"]):
+            assert_places(field[tuple(idx)], exp)
