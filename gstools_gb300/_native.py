@@ -54,6 +54,8 @@ SIGNATURES = {
     "gst_summate_incompr_grid_mixed": (_c_int, [_c_int, _i64, _ptr, _ptr,
                                                 _ptr, _ptr, _ptr, _ptr, _c_int,
                                                 _dbl, _ptr]),
+    "gst_summate_grid_tc": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr, _ptr,
+                                     _ptr, _ptr, _c_int, _dbl, _ptr]),
     "gst_peak_probe": (_c_int, [_c_int, _i64, _ptr, ctypes.POINTER(_dbl),
                                 _ptr]),
 }

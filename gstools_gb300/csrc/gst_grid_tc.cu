@@ -1,0 +1,598 @@
+// Separable structured-grid summation on the sm_103a tensor cores (tcgen05).
+//
+// On a structured grid the phase separates per axis, exp(i<k, x>) =
+// Ex[ix] Ey[iy] Ez[iz], so with w_j = z1_j - i z2_j the reference sum
+// (src/gstools/field/generator.py:193-199 on the meshgrid of
+// src/gstools/tools/geometric.py:340-356) becomes
+//
+//     F[ix, iy, iz] = Re sum_j (w_j Ex[ix, j]) (Ey[iy, j] Ez[iz, j])
+//                   = sum_K A[ix, K] B[(iy, iz), K]
+//
+// a real GEMM with K = 2N (real and imaginary parts), A = [Re(w Ex),
+// -Im(w Ex)] over the x axis and B = [Re(Ey Ez), Im(Ey Ez)] the Khatri-Rao
+// product over the (y, z) pairs.  A linear isometrize map M is folded into
+// the wave vectors by the caller (<k, M x> = <M^T k, x>).
+//
+// Precision: the per-axis tables come from an exact FP64 turn reduction of
+// k x / (2 pi) and an FP32 sincospi of the reduced angle; every operand is
+// split into TF32 hi + lo and the GEMM runs as Ah Bh + Ah Bl + Al Bh
+// (3xTF32).  The tensor core's FP32 accumulation is not round-to-nearest
+// over long K (its error grows with the number of MMAs added into one large
+// running sum), so the modes are processed in chunks of 32: each chunk
+// accumulates from zero in tensor memory and is then added into FP32
+// registers of the epilogue threads.  Two accumulators alternate, so the
+// tensor cores fill one while the other is drained.
+//
+// Kernel structure (one CTA per output tile of 128 x-rows by 256 (y, z)
+// points, 320 threads):
+//   warp 0      bulk-copy (TMA) producer: per stage the pre-split A image
+//               (16 KB, already in the UMMA canonical K-major layout) and the
+//               stage's Ey / Ez table slices;
+//   warp 1      allocates 512 TMEM columns (two 128 x 256 FP32 accumulators)
+//               and issues tcgen05.mma from one thread, M=128 N=256 K=8,
+//               3 MMAs per K-step;
+//   warps 2-9   generate B = Ey * Ez (complex product, TF32 split) into the
+//               stage's shared memory, drain finished chunk accumulators
+//               into registers (tcgen05.ld), and store the scaled tile.
+// Every mbarrier wait is bounded (gst::mbar_wait); a timeout is recorded in
+// the device error word and the CTA still frees its tensor memory.
+#include <algorithm>
+
+#include "gst_common.cuh"
+
+namespace gst {
+namespace {
+
+constexpr int kThreads = 320;
+constexpr int kGenThreads = 256;      // warps 2-9
+constexpr int kTileCols = 256;        // (y, z) points per tile (MMA N)
+constexpr int kXBlock = 128;          // x rows per tile (MMA M)
+constexpr int kModesPerKStep = 4;     // 8 reals = K of one tf32 MMA
+constexpr int kKSteps = 2;            // K-steps per pipeline stage
+constexpr int kModesPerStage = kModesPerKStep * kKSteps;
+constexpr int kABlockBytes = 128 * 8 * 4;           // 128 rows x 8 tf32
+constexpr int kBBlockBytes = kTileCols * 8 * 4;     // 256 rows x 8 tf32
+constexpr int kAStageBytes = kKSteps * 2 * kABlockBytes;      // 16 KB
+constexpr int kBStageBytes = kKSteps * 2 * kBBlockBytes;      // 32 KB
+constexpr uint32_t kTmemCols = 512;  // two 256-column accumulators
+constexpr int kChunkStages = 4;      // 32 modes accumulate per chunk
+constexpr int kColsPerThread = 128;  // epilogue: half a row of 256 columns
+
+constexpr double kInv2Pi = 0.15915494309189533576888376337251436;
+
+// Byte offset of element (row, k) inside one canonical K-major block of
+// 8-row x 16-byte core matrices: core (row/8, k/4) sits at
+// (row/8) * SBO + (k/4) * LBO with LBO = 128 B, SBO = 256 B.
+__host__ __device__ constexpr uint32_t core_offset(uint32_t row, uint32_t k) {
+    return (row >> 3) * 256u + (k >> 2) * 128u + (row & 7u) * 16u + (k & 3u) * 4u;
+}
+
+__device__ __forceinline__ float to_tf32(float v) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+    return __uint_as_float(r);
+}
+
+// ------------------------------------------------------------ descriptors --
+
+// tcgen05 shared-memory matrix descriptor, K-major, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);          // start
+    d |= static_cast<uint64_t>((128u >> 4) & 0x3FFFu) << 16;     // LBO
+    d |= static_cast<uint64_t>((256u >> 4) & 0x3FFFu) << 32;     // SBO
+    d |= static_cast<uint64_t>(1u) << 46;                        // version
+    return d;                                                    // swizzle 0
+}
+
+// Instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major,
+// M = 128, N = 256.
+constexpr uint32_t kIdesc = (1u << 4)            // D format F32
+                            | (2u << 7)          // A format TF32
+                            | (2u << 10)         // B format TF32
+                            | ((256u >> 3) << 17)  // N
+                            | ((128u >> 4) << 24); // M
+
+// ------------------------------------------------------------- tcgen05 ops --
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+            smem_addr(dst_smem)),
+        "r"(ncols)
+        : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::
+                     : "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
+                     taddr),
+                 "r"(ncols)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc,
+                                         uint64_t b_desc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+            d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
+        "[%0];" ::"r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
+// 32 lanes x 32 consecutive FP32 columns of tensor memory.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, "
+        "%29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]),
+          "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+          "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+          "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ------------------------------------------------------------------ tables --
+
+struct GridGeom {
+    int64_t n[3];        // axis lengths (n[2] = 1 for 2-D)
+    int64_t off[3];      // offsets of the axes in the concatenated array
+    int64_t blocks[3];   // tiles along x (256), y (TY), z (TZ)
+    int tile[3];         // 256, TY, TZ
+    int64_t n_stages;    // padded modes / kModesPerStage
+    int64_t n_modes;
+};
+
+// One thread per (axis row, mode).  Axis 0 writes the pre-split A image,
+// axes 1 and 2 the complex tables Ey, Ez in per-stage blocks.
+__global__ void grid_tables_kernel(GridGeom g, int dim,
+                                   const double *__restrict__ cov,
+                                   const double *__restrict__ z1,
+                                   const double *__restrict__ z2,
+                                   const double *__restrict__ axes,
+                                   unsigned char *__restrict__ a_image,
+                                   float2 *__restrict__ ey,
+                                   float2 *__restrict__ ez) {
+    const int axis = blockIdx.z;
+    const int64_t n_pad_modes = g.n_stages * kModesPerStage;
+    const int64_t rows = g.blocks[axis] * g.tile[axis];
+    const int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (idx >= rows * n_pad_modes) return;
+    const int64_t j = idx % n_pad_modes;
+    const int64_t r = idx / n_pad_modes;
+
+    float c = 0.0f, s = 0.0f;
+    const bool live = (j < g.n_modes) && (r < g.n[axis]) &&
+                      (axis < dim || axis == 2);
+    if (live) {
+        double k = 0.0, x = 0.0;
+        if (axis < dim) {
+            k = cov[axis * g.n_modes + j];
+            x = axes[g.off[axis] + r];
+        }
+        // exact reduction of the phase to turns, FP32 sin/cos of the rest
+        const double t = (k * kInv2Pi) * x;
+        const double frac = t - rint(t);
+        sincospif(2.0f * static_cast<float>(frac), &s, &c);
+    }
+    const int64_t st = j / kModesPerStage;
+    const int mm = static_cast<int>(j % kModesPerStage);
+    if (axis == 0) {
+        // a = w E with w = z1 - i z2: Re a = z1 c + z2 s, -Im a = z2 c - z1 s
+        float re = 0.0f, nim = 0.0f;
+        if (live) {
+            const double zz1 = z1[j], zz2 = z2[j];
+            re = static_cast<float>(zz1 * c + zz2 * s);
+            nim = static_cast<float>(zz2 * c - zz1 * s);
+        }
+        const int64_t xb = r / kXBlock;
+        const uint32_t row = static_cast<uint32_t>(r % kXBlock);
+        const int kstep = mm / kModesPerKStep;
+        const uint32_t k0 = 2u * (mm % kModesPerKStep);
+        unsigned char *stage = a_image + (xb * g.n_stages + st) * kAStageBytes;
+        const float vals[2] = {re, nim};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const float hi = to_tf32(vals[q]);
+            const float lo = to_tf32(vals[q] - hi);
+            const uint32_t o = core_offset(row, k0 + q);
+            *reinterpret_cast<float *>(stage + (kstep * 2 + 0) * kABlockBytes +
+                                       o) = hi;
+            *reinterpret_cast<float *>(stage + (kstep * 2 + 1) * kABlockBytes +
+                                       o) = lo;
+        }
+    } else {
+        const int tile = g.tile[axis];
+        const int64_t blk = r / tile;
+        const int t = static_cast<int>(r % tile);
+        float2 *tab = (axis == 1) ? ey : ez;
+        tab[((blk * g.n_stages + st) * kModesPerStage + mm) * tile + t] =
+            make_float2(c, s);
+    }
+}
+
+// -------------------------------------------------------------- main kernel --
+
+__device__ __forceinline__ int64_t ceil_div_dev(int64_t a, int64_t b) {
+    return (a + b - 1) / b;
+}
+
+struct GridArgs {
+    GridGeom g;
+    const unsigned char *a_image;
+    const float2 *ey;
+    const float2 *ez;
+    void *out;
+    int out_f32;
+    double scale;
+    unsigned int *err;
+};
+
+template <int TY>
+struct StageLayout {
+    static constexpr int TZ = kTileCols / TY;
+    static constexpr int kEyBytes = kModesPerStage * TY * 8;
+    static constexpr int kEzBytes = kModesPerStage * TZ * 8;
+    static constexpr int kA = 0;
+    static constexpr int kEy = kA + kAStageBytes;
+    static constexpr int kEz = kEy + kEyBytes;
+    static constexpr int kB = (kEz + kEzBytes + 1023) / 1024 * 1024;
+    static constexpr int kBytes = kB + kBStageBytes;
+    static constexpr int kCopyBytes = kAStageBytes + kEyBytes + kEzBytes;
+    static constexpr int kPipe = (4 * kBytes + 2048 <= 227 * 1024) ? 4 : 3;
+    static constexpr int kSmem = kPipe * kBytes + 1024 /*align*/ + 256 /*bars*/;
+};
+
+template <int TY>
+__global__ void __launch_bounds__(kThreads, 1)
+    grid_tc_kernel(const GridArgs a) {
+    using L = StageLayout<TY>;
+    constexpr int TZ = L::TZ;
+    constexpr int P = L::kPipe;
+
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + P * L::kBytes);
+    uint64_t *full = bars;           // [P] bulk copies landed
+    uint64_t *bready = bars + P;     // [P] B generated
+    uint64_t *empty = bars + 2 * P;  // [P] MMAs done with the stage
+    uint64_t *chunk_done = bars + 3 * P;     // [2] accumulator b complete
+    uint64_t *acc_free = bars + 3 * P + 2;   // [2] accumulator b drained
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 3 * P + 4);
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const GridGeom &g = a.g;
+
+    const int64_t tile = blockIdx.x;
+    const int64_t zb = tile % g.blocks[2];
+    const int64_t yb = (tile / g.blocks[2]) % g.blocks[1];
+    const int64_t xb = tile / (g.blocks[2] * g.blocks[1]);
+    const int64_t n_st = g.n_stages;
+    const int64_t n_chunks = ceil_div_dev(n_st, kChunkStages);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < P; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&bready[s], kGenThreads / 32);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&chunk_done[b], 1);
+            mbar_init(&acc_free[b], kGenThreads / 32);
+        }
+        fence_mbar_init();
+    }
+    if (warp == 1) tmem_alloc(tmem_slot, kTmemCols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    bool ok = true;
+    if (warp == 0) {
+        // ---------------------------------------------- bulk producer --
+        if (lane == 0) {
+            const unsigned char *a_src = a.a_image + xb * n_st * kAStageBytes;
+            const float2 *ey_src = a.ey + yb * n_st * kModesPerStage * TY;
+            const float2 *ez_src = a.ez + zb * n_st * kModesPerStage * TZ;
+            for (int64_t st = 0; st < n_st && ok; ++st) {
+                const int s = static_cast<int>(st % P);
+                const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
+                ok = mbar_wait(&empty[s], ph ^ 1u, a.err);
+                if (!ok) break;
+                unsigned char *dst = smem + s * L::kBytes;
+                mbar_arrive_expect_tx(&full[s], L::kCopyBytes);
+                bulk_copy_g2s(dst + L::kA, a_src + st * kAStageBytes,
+                              kAStageBytes, &full[s]);
+                bulk_copy_g2s(dst + L::kEy, ey_src + st * kModesPerStage * TY,
+                              L::kEyBytes, &full[s]);
+                bulk_copy_g2s(dst + L::kEz, ez_src + st * kModesPerStage * TZ,
+                              L::kEzBytes, &full[s]);
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------- MMA issuer --
+        if (lane == 0) {
+            for (int64_t st = 0; st < n_st && ok; ++st) {
+                const int s = static_cast<int>(st % P);
+                const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
+                const int64_t c = st / kChunkStages;
+                const int buf = static_cast<int>(c & 1);
+                const bool first = (st % kChunkStages) == 0;
+                if (first && c >= 2) {
+                    // accumulator reused: wait until chunk c-2 was drained
+                    ok = mbar_wait(&acc_free[buf],
+                                   static_cast<uint32_t>(((c >> 1) - 1) & 1), a.err);
+                    if (!ok) break;
+                }
+                ok = mbar_wait(&full[s], ph, a.err) &&
+                     mbar_wait(&bready[s], ph, a.err);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t base = smem_addr(smem + s * L::kBytes);
+                const uint32_t d = tmem + buf * 256;
+#pragma unroll
+                for (int ks = 0; ks < kKSteps; ++ks) {
+                    const uint64_t bh = smem_desc(base + L::kB + (ks * 2 + 0) * kBBlockBytes);
+                    const uint64_t bl = smem_desc(base + L::kB + (ks * 2 + 1) * kBBlockBytes);
+                    const uint32_t ablk = base + L::kA + ks * 2 * kABlockBytes;
+                    const uint64_t ah = smem_desc(ablk);
+                    const uint64_t al = smem_desc(ablk + kABlockBytes);
+                    const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+                    mma_tf32(d, ah, bh, acc);
+                    mma_tf32(d, ah, bl, 1u);
+                    mma_tf32(d, al, bh, 1u);
+                }
+                mma_commit(&empty[s]);
+                if ((st % kChunkStages) == kChunkStages - 1 || st == n_st - 1)
+                    mma_commit(&chunk_done[buf]);
+            }
+        }
+    } else {
+        // ------------------------------------- B generators + epilogue --
+        const int gt = threadIdx.x - 64;       // 0..255: row of the B tile
+        const int yl = gt / TZ, zl = gt % TZ;
+        const int q = warp & 3;                // TMEM lane quarter
+        const int half = (warp - 2) >> 2;      // accumulator columns half
+        const uint32_t t_row = tmem + (static_cast<uint32_t>(q * 32) << 16) +
+                               half * kColsPerThread;
+        float acc[kColsPerThread];
+#pragma unroll
+        for (int i = 0; i < kColsPerThread; ++i) acc[i] = 0.0f;
+        int64_t drained = 0;
+
+        // Adds chunk `c` (accumulator c & 1) into the registers and frees it.
+        auto drain = [&](int64_t c) -> bool {
+            const int buf = static_cast<int>(c & 1);
+            const bool got = __all_sync(
+                0xffffffffu,
+                mbar_wait(&chunk_done[buf], static_cast<uint32_t>((c >> 1) & 1),
+                          a.err));
+            if (!got) return false;
+            tc_fence_after();
+#pragma unroll
+            for (int j = 0; j < kColsPerThread / 32; ++j) {
+                float v[32];
+                tmem_ld32(t_row + buf * 256 + j * 32, v);
+#pragma unroll
+                for (int i = 0; i < 32; ++i) acc[j * 32 + i] += v[i];
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_free[buf]);
+            return true;
+        };
+
+        for (int64_t st = 0; st < n_st && ok; ++st) {
+            const int s = static_cast<int>(st % P);
+            const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
+            ok = mbar_wait(&full[s], ph, a.err);
+            if (__any_sync(0xffffffffu, !ok)) { ok = false; break; }
+            unsigned char *stage = smem + s * L::kBytes;
+            const float2 *sey = reinterpret_cast<const float2 *>(stage + L::kEy);
+            const float2 *sez = reinterpret_cast<const float2 *>(stage + L::kEz);
+#pragma unroll
+            for (int ks = 0; ks < kKSteps; ++ks) {
+                float hi[8], lo[8];
+#pragma unroll
+                for (int m = 0; m < kModesPerKStep; ++m) {
+                    const int mm = ks * kModesPerKStep + m;
+                    const float2 p = sey[mm * TY + yl];
+                    const float2 r = sez[mm * TZ + zl];
+                    const float re = fmaf(p.x, r.x, -p.y * r.y);
+                    const float im = fmaf(p.x, r.y, p.y * r.x);
+                    hi[2 * m] = to_tf32(re);
+                    lo[2 * m] = to_tf32(re - hi[2 * m]);
+                    hi[2 * m + 1] = to_tf32(im);
+                    lo[2 * m + 1] = to_tf32(im - hi[2 * m + 1]);
+                }
+                unsigned char *bh = stage + L::kB + (ks * 2 + 0) * kBBlockBytes;
+                unsigned char *bl = stage + L::kB + (ks * 2 + 1) * kBBlockBytes;
+#pragma unroll
+                for (int kb = 0; kb < 2; ++kb) {
+                    const uint32_t o = core_offset(gt, kb * 4);
+                    *reinterpret_cast<float4 *>(bh + o) = make_float4(
+                        hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
+                    *reinterpret_cast<float4 *>(bl + o) = make_float4(
+                        lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
+                }
+            }
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bready[s]);
+            // Drain the previous chunk once the MMAs are past it: the
+            // generators run at most P stages ahead of the tensor cores.
+            if (drained < n_chunks - 1 &&
+                st == (drained + 1) * kChunkStages - 1 + (P - 1)) {
+                ok = drain(drained);
+                ++drained;
+            }
+        }
+        for (; drained < n_chunks && ok; ++drained) ok = drain(drained);
+
+        if (ok) {
+            const int64_t x = xb * kXBlock + q * 32 + lane;
+            const int64_t ny = g.n[1], nz = g.n[2];
+            if (x < g.n[0]) {
+#pragma unroll
+                for (int i = 0; i < kColsPerThread; ++i) {
+                    const int n = half * kColsPerThread + i;
+                    const int64_t y = yb * TY + n / TZ;
+                    const int64_t z = zb * TZ + n % TZ;
+                    if (y < ny && z < nz) {
+                        const int64_t o = (x * ny + y) * nz + z;
+                        if (a.out_f32)
+                            static_cast<float *>(a.out)[o] =
+                                static_cast<float>(a.scale * acc[i]);
+                        else
+                            static_cast<double *>(a.out)[o] = a.scale * acc[i];
+                    }
+                }
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        tc_fence_after();
+        tmem_dealloc(tmem, kTmemCols);
+    }
+}
+
+template <int TY>
+cudaError_t launch_grid(const GridArgs &args, int64_t n_tiles, cudaStream_t s) {
+    using L = StageLayout<TY>;
+    cudaError_t e = cudaFuncSetAttribute(grid_tc_kernel<TY>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         L::kSmem);
+    if (e != cudaSuccess) return e;
+    grid_tc_kernel<TY><<<static_cast<unsigned>(n_tiles), kThreads, L::kSmem, s>>>(args);
+    return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace gst
+
+extern "C" int gst_summate_grid_tc(int dim, int64_t n_modes,
+                                   const int64_t *axis_len, const double *axes,
+                                   const double *cov_samples, const double *z_1,
+                                   const double *z_2, void *out, int out_type,
+                                   double scale, void *stream) {
+    using namespace gst;
+    if (dim < 2 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
+    if (axis_len == nullptr || n_modes < 0) return GST_ERR_INVALID_ARGUMENT;
+    if (out_type != GST_OUT_F64 && out_type != GST_OUT_F32)
+        return GST_ERR_INVALID_ARGUMENT;
+    GridGeom g{};
+    int64_t total = 1, off = 0;
+    for (int d = 0; d < 3; ++d) {
+        g.n[d] = d < dim ? axis_len[d] : 1;
+        if (g.n[d] < 0) return GST_ERR_INVALID_ARGUMENT;
+        g.off[d] = off;
+        off += d < dim ? g.n[d] : 0;
+        total *= g.n[d];
+    }
+    if (total == 0) return GST_OK;
+    if (out == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    if (current_device() < 0) return GST_ERR_NO_DEVICE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t elem = out_type == GST_OUT_F32 ? 4 : 8;
+    if (n_modes == 0) {
+        GST_TRY_CUDA(cudaMemsetAsync(out, 0, elem * total, s));
+        return GST_OK;
+    }
+    if (cov_samples == nullptr || z_1 == nullptr || z_2 == nullptr ||
+        axes == nullptr)
+        return GST_ERR_INVALID_ARGUMENT;
+
+    const int ty = dim == 3 ? 16 : kTileCols;
+    const int tz = kTileCols / ty;
+    g.tile[0] = kXBlock;
+    g.tile[1] = ty;
+    g.tile[2] = tz;
+    for (int d = 0; d < 3; ++d) g.blocks[d] = ceil_div(g.n[d], g.tile[d]);
+    g.n_stages = ceil_div(n_modes, kModesPerStage);
+    g.n_modes = n_modes;
+    const int64_t n_tiles = g.blocks[0] * g.blocks[1] * g.blocks[2];
+    if (n_tiles > 0x7fffffffLL) return GST_ERR_TOO_LARGE;
+
+    const size_t a_bytes = static_cast<size_t>(g.blocks[0]) * g.n_stages * kAStageBytes;
+    const size_t ey_bytes = static_cast<size_t>(g.blocks[1]) * g.n_stages *
+                            kModesPerStage * ty * sizeof(float2);
+    const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages *
+                            kModesPerStage * tz * sizeof(float2);
+    const size_t ey_off = align_up(a_bytes, 256);
+    const size_t ez_off = align_up(ey_off + ey_bytes, 256);
+    unsigned int *err = device_error_word();
+    if (err == nullptr) return GST_ERR_CUDA;
+
+    StreamScratch ws;
+    GST_TRY_CUDA(ws.alloc(ez_off + ez_bytes, s));
+    unsigned char *base = static_cast<unsigned char *>(ws.ptr);
+
+    const int64_t n_pad_modes = g.n_stages * kModesPerStage;
+    int64_t max_rows = 0;
+    for (int d = 0; d < 3; ++d) max_rows = std::max(max_rows, g.blocks[d] * g.tile[d]);
+    const int threads = 256;
+    const dim3 tgrid(static_cast<unsigned>(ceil_div(max_rows * n_pad_modes, threads)), 1, 3);
+    grid_tables_kernel<<<tgrid, threads, 0, s>>>(
+        g, dim, cov_samples, z_1, z_2, axes, base,
+        reinterpret_cast<float2 *>(base + ey_off),
+        reinterpret_cast<float2 *>(base + ez_off));
+    GST_TRY_CUDA(cudaGetLastError());
+
+    GridArgs args{};
+    args.g = g;
+    args.a_image = base;
+    args.ey = reinterpret_cast<const float2 *>(base + ey_off);
+    args.ez = reinterpret_cast<const float2 *>(base + ez_off);
+    args.out = out;
+    args.out_f32 = out_type == GST_OUT_F32 ? 1 : 0;
+    args.scale = scale;
+    args.err = err;
+    const cudaError_t e = (ty == 16) ? launch_grid<16>(args, n_tiles, s)
+                                     : launch_grid<kTileCols>(args, n_tiles, s);
+    GST_TRY_CUDA(e);
+    return GST_OK;
+}

@@ -13,8 +13,9 @@
 //   * a tile of evaluation points lives in registers for the whole kernel
 //     (P points per thread, coalesced loads, one pass over HBM);
 //   * the mode set has been packed by a prologue kernel into a table of
-//     64-byte entries (wave vector pre-divided by pi or 2*pi, amplitudes,
-//     projector) padded with zero-amplitude modes to a whole number of tiles;
+//     64-byte entries (FP64 wave vector, or its split FP32 turns for the
+//     mixed path; amplitudes; projector) padded with zero-amplitude modes to
+//     a whole number of tiles;
 //   * mode tiles stream into shared memory through double-buffered bulk (TMA)
 //     copies tracked by mbarriers, and every thread reads each entry as a
 //     broadcast;
@@ -58,12 +59,20 @@ constexpr double kPi = 3.141592653589793238462643383279502884;
 
 // ---------------------------------------------------------- mode packing --
 //
-// FP64 scalar entry  (8 doubles): q0 q1 q2 q3 z1 z2 - -     q = k / pi
-// FP64 incompr entry (8 doubles): q0 q1 q2 z1 z2 p0 p1 p2   p = projector
+// FP64 scalar entry  (8 doubles): k0 k1 k2 k3 z1 z2 f -    f = weight (1)
+// FP64 incompr entry (8 doubles): k0 k1 k2 z1 z2 p0 p1 p2   p = projector
 // mixed entry (16 floats): qh0 qh1 qh2 z1 | ql0 ql1 ql2 z2 | p0 p1 p2 - | ...
 //                          q = k / (2 pi) split as qh (12 significant bits)
 //                          + ql, so qh * xh is exact in FP32.
-// `weight` (summate_fourier's spectrum factor) multiplies z1 and z2.
+// `weight` is summate_fourier's spectrum factor: the FP64 table keeps it as a
+// separate factor (applied to z1 cos + z2 sin, as the reference does); the
+// mixed table folds it into z1 and z2.
+//
+// The FP64 path evaluates every (mode, point) pair in the reference's own
+// operation order -- phase = ((k0 x0) + k1 x1) + ..., each product and sum
+// rounded separately (no FMA contraction), sin/cos of the radian phase,
+// acc += (z1 cos + z2 sin) -- so it tracks the reference to a few ulp even
+// where phases reach 1e5 rad.
 
 template <int KIND, int PREC>
 __global__ void pack_modes_kernel(int dim, int64_t n_modes, int64_t n_padded,
@@ -75,36 +84,39 @@ __global__ void pack_modes_kernel(int dim, int64_t n_modes, int64_t n_padded,
     const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (j >= n_padded) return;
     double k[4] = {0.0, 0.0, 0.0, 0.0};
-    double a1 = 0.0, a2 = 0.0;
+    double a1 = 0.0, a2 = 0.0, w = 0.0;
     double proj[3] = {0.0, 0.0, 0.0};
     if (j < n_modes) {
         for (int d = 0; d < dim; ++d) k[d] = cov[d * n_modes + j];
-        const double w = weight ? weight[j] : 1.0;
-        a1 = weight ? w * z1[j] : z1[j];
-        a2 = weight ? w * z2[j] : z2[j];
+        w = weight ? weight[j] : 1.0;
+        a1 = z1[j];
+        a2 = z2[j];
         if (KIND == kIncompr) {
             // p_c = delta_c0 - k_c k_0 / |k|^2   (generator.py:479-495)
             double k2 = 0.0;
-            for (int d = 0; d < dim; ++d) k2 += k[d] * k[d];
+            for (int d = 0; d < dim; ++d) k2 = __dadd_rn(k2, __dmul_rn(k[d], k[d]));
             for (int d = 0; d < dim; ++d)
-                proj[d] = (d == 0 ? 1.0 : 0.0) - k[d] * k[0] / k2;
+                proj[d] = __dsub_rn(d == 0 ? 1.0 : 0.0,
+                                    __ddiv_rn(__dmul_rn(k[d], k[0]), k2));
         }
     }
     if (PREC == kF64) {
         double *e = static_cast<double *>(table) + j * 8;
         if (KIND == kScalar) {
-            for (int d = 0; d < 4; ++d) e[d] = k[d] / kPi;
+            for (int d = 0; d < 4; ++d) e[d] = k[d];
             e[4] = a1;
             e[5] = a2;
-            e[6] = 0.0;
+            e[6] = w;
             e[7] = 0.0;
         } else {
-            for (int d = 0; d < 3; ++d) e[d] = k[d] / kPi;
+            for (int d = 0; d < 3; ++d) e[d] = k[d];
             e[3] = a1;
             e[4] = a2;
             for (int d = 0; d < 3; ++d) e[5 + d] = proj[d];
         }
     } else {
+        a1 *= w;
+        a2 *= w;
         float *e = static_cast<float *>(table) + j * 16;
         for (int d = 0; d < 3; ++d) {
             const double q = k[d] / (2.0 * kPi);
@@ -230,32 +242,28 @@ __global__ void __launch_bounds__(Tiling<PREC>::kThreads,
 
         if (PREC == kF64) {
             const double *e = reinterpret_cast<const double *>(stage[s]);
-#pragma unroll 2
+#pragma unroll 1
             for (int jj = 0; jj < TILE; ++jj, e += 8) {
-                if (KIND == kScalar) {
-                    const double2 za = *reinterpret_cast<const double2 *>(e + 4);
+                const double z1 = (KIND == kScalar) ? e[4] : e[3];
+                const double z2 = (KIND == kScalar) ? e[5] : e[4];
 #pragma unroll
-                    for (int p = 0; p < P; ++p) {
-                        double u = e[0] * x[p][0];
+                for (int p = 0; p < P; ++p) {
+                    // reference order: phase += k_d * x_d, unfused
+                    double ph = __dmul_rn(e[0], x[p][0]);
 #pragma unroll
-                        for (int d = 1; d < DIM; ++d) u = fma(e[d], x[p][d], u);
-                        double sn, cs;
-                        sincospi(u, &sn, &cs);
-                        acc[p][0] = fma(za.x, cs, fma(za.y, sn, acc[p][0]));
-                    }
-                } else {
-                    const double z1 = e[3], z2 = e[4];
-#pragma unroll
-                    for (int p = 0; p < P; ++p) {
-                        double u = e[0] * x[p][0];
-#pragma unroll
-                        for (int d = 1; d < DIM; ++d) u = fma(e[d], x[p][d], u);
-                        double sn, cs;
-                        sincospi(u, &sn, &cs);
-                        const double amp = fma(z1, cs, z2 * sn);
+                    for (int d = 1; d < DIM; ++d)
+                        ph = __dadd_rn(ph, __dmul_rn(e[d], x[p][d]));
+                    double sn, cs;
+                    sincos(ph, &sn, &cs);
+                    const double amp =
+                        __dadd_rn(__dmul_rn(z1, cs), __dmul_rn(z2, sn));
+                    if (KIND == kScalar) {
+                        acc[p][0] = __dadd_rn(acc[p][0], __dmul_rn(e[6], amp));
+                    } else {
 #pragma unroll
                         for (int c = 0; c < NC; ++c)
-                            acc[p][c] = fma(e[5 + c], amp, acc[p][c]);
+                            acc[p][c] =
+                                __dadd_rn(acc[p][c], __dmul_rn(e[5 + c], amp));
                     }
                 }
             }

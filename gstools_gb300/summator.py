@@ -194,15 +194,36 @@ def summate_grid(cov_samples, z_1, z_2, axes, *, precision=None,
     ``cov_samples`` must already be multiplied by ``M^T`` when the reference
     would isometrize the grid with ``M``.  Returns an array of shape
     ``tuple(len(a) for a in axes)``; ``scale`` multiplies the result.
-    ``method`` picks the kernel: "pointwise" (per-point phases) or "auto".
+
+    ``method`` picks the kernel:
+
+    * ``"pointwise"`` -- per-point phases (FP64 or mixed, per ``precision``);
+    * ``"tensor"``    -- the separable 3xTF32 tensor-core contraction (2-D and
+      3-D grids, requires ``precision="mixed"``);
+    * ``"auto"``      -- ``"tensor"`` for mixed precision on 2-D / 3-D grids,
+      ``"pointwise"`` otherwise.
     """
     prec = config.check_precision(precision)
+    if method not in ("auto", "pointwise", "tensor"):
+        raise ValueError(f"unknown method {method!r}")
     as_torch = _is_torch(cov_samples, z_1, z_2, *axes)
     dev, cov, z1, z2, flat, lens, shape = _prepare_grid(cov_samples, z_1,
                                                         z_2, axes)
     dim, n_modes = cov.shape
     stream = _stream(dev)
-    if prec == "f64":
+    if method == "auto":
+        method = "tensor" if (prec == "mixed" and dim in (2, 3)) else "pointwise"
+    if method == "tensor":
+        if prec != "mixed":
+            raise ValueError("the tensor-core grid path is mixed precision")
+        if dim not in (2, 3):
+            raise ValueError("the tensor-core grid path needs a 2-D or 3-D grid")
+        code, tdtype = _out_type(out_dtype)
+        out = torch.empty(shape, dtype=tdtype, device=dev)
+        _native.call("gst_summate_grid_tc", dim, n_modes, lens, _p(flat),
+                     _p(cov), _p(z1), _p(z2), _p(out), code, float(scale),
+                     stream)
+    elif prec == "f64":
         out = torch.empty(shape, dtype=torch.float64, device=dev)
         _native.call("gst_summate_grid_f64", dim, n_modes, lens, _p(flat),
                      _p(cov), _p(z1), _p(z2), _p(out), stream)

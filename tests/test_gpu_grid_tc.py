@@ -1,0 +1,97 @@
+"""GPU parity of the separable tensor-core grid path (3xTF32, tcgen05).
+
+Bar: RMS(gpu - oracle) of the scaled field <= 1e-5 sigma (sigma = sqrt(var),
+field scaled by sqrt(var / N)), and max error <= 1e-4 sigma.
+"""
+
+import numpy as np
+import pytest
+
+import gstools_gb300 as gg
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+RMS_SIGMA = 1e-5
+MAX_SIGMA = 1e-4
+
+
+def grid_ref(cov, z1, z2, axes):
+    grid = np.array(np.meshgrid(*axes, indexing="ij")).reshape(len(axes), -1)
+    return oracle.c_summate(cov, z1, z2, grid).reshape([len(a) for a in axes])
+
+
+def errors(got, ref, n_modes, var=1.0):
+    d = np.sqrt(var / n_modes) * (np.asarray(got, dtype=np.float64) - ref)
+    return (np.sqrt(np.mean(d**2)) / np.sqrt(var),
+            np.max(np.abs(d)) / np.sqrt(var))
+
+
+def case(seed, dim, n_modes, k_scale=0.2):
+    rng = np.random.RandomState(seed)
+    cov = rng.standard_t(3, size=(dim, n_modes)) * k_scale
+    return cov, rng.normal(size=n_modes), rng.normal(size=n_modes)
+
+
+@pytest.mark.parametrize("shape,n_modes", [
+    ((16, 16), 8), ((256, 256), 64), ((37, 300), 13), ((300, 5), 100),
+    ((1, 1), 1), ((513, 17), 203)])
+def test_tc_2d(cuda_lib, shape, n_modes):
+    cov, z1, z2 = case(sum(shape) + n_modes, 2, n_modes)
+    axes = [np.linspace(-20.0, 80.0, shape[0]), np.arange(shape[1]) * 0.7]
+    ref = grid_ref(cov, z1, z2, axes)
+    got = gg.summate_grid(cov, z1, z2, axes, precision="mixed",
+                          method="tensor", out_dtype="float32")
+    assert got.shape == shape and got.dtype == np.float32
+    rms, mx = errors(got, ref, n_modes)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (rms, mx)
+
+
+@pytest.mark.parametrize("shape,n_modes", [
+    ((16, 16, 16), 8), ((20, 33, 17), 61), ((256, 16, 16), 500),
+    ((3, 40, 70), 1000), ((300, 9, 31), 37)])
+def test_tc_3d(cuda_lib, shape, n_modes):
+    cov, z1, z2 = case(sum(shape) * 3 + n_modes, 3, n_modes)
+    axes = [np.arange(float(shape[0])), np.arange(shape[1]) * 1.5 - 7.0,
+            np.linspace(0.0, 50.0, shape[2])]
+    ref = grid_ref(cov, z1, z2, axes)
+    got = gg.summate_grid(cov, z1, z2, axes, precision="mixed",
+                          method="tensor")
+    assert got.shape == shape and got.dtype == np.float64
+    rms, mx = errors(got, ref, n_modes)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (rms, mx)
+
+
+def test_tc_exp3d_workload_slab(cuda_lib, workloads):
+    """The benchmark's modes (3-D anisotropic Exponential, 2000 modes) on a
+    full 256^3 grid, checked against the oracle on scattered slabs."""
+    c = workloads.case("exp3d")
+    kp = c["isometrize"].T @ c["cov"]
+    axes = [np.arange(256.0)] * 3
+    full = gg.summate_grid(kp, c["z1"], c["z2"], axes, precision="mixed",
+                           method="tensor", out_dtype="float32")
+    assert full.shape == (256, 256, 256)
+    for ix in (0, 77, 255):
+        sub = [axes[0][ix:ix + 1], axes[1][::5], axes[2][::3]]
+        ref = grid_ref(kp, c["z1"], c["z2"], sub)
+        got = full[ix:ix + 1, ::5, ::3]
+        rms, mx = errors(got, ref, 2000, var=2.0)
+        assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (ix, rms, mx)
+
+
+def test_tc_scale_and_zero_modes(cuda_lib):
+    cov, z1, z2 = case(5, 3, 40)
+    axes = [np.arange(10.0), np.arange(12.0), np.arange(14.0)]
+    a = gg.summate_grid(cov, z1, z2, axes, precision="mixed", method="tensor")
+    b = gg.summate_grid(cov, z1, z2, axes, precision="mixed", method="tensor",
+                        scale=0.25)
+    np.testing.assert_allclose(b, 0.25 * a, rtol=1e-6, atol=1e-9)
+    z = gg.summate_grid(np.zeros((3, 0)), np.zeros(0), np.zeros(0), axes,
+                        precision="mixed", method="tensor")
+    np.testing.assert_array_equal(z, np.zeros((10, 12, 14)))
+
+
+def test_tc_no_device_error(cuda_lib):
+    from gstools_gb300 import _native
+
+    assert _native.read_device_error() == 0
