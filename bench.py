@@ -9,12 +9,15 @@ evaluations per step.
 Metric: G mode*point evals/s of the fastest path at its stated error against
 the FP64 kernel, with the plain FP64 kernel's throughput reported beside it.
 
-* ``value``  -- device-resident inputs, CUDA-event timing of the summation
-                alone (L2 flushed between steps);
+* ``value``  -- device-resident inputs, CUDA-event timing of one step of the
+                separable tensor-core path (per-axis tables + 3xTF32
+                contraction; L2 flushed between steps);
 * ``e2e``    -- the public API ``gstools_gb300.summate_grid`` called with host
                 numpy arrays: host->device copy of the modes and axes, the
                 kernels, and the device->host copy of the float32 field, all
                 inside the timed region;
+* ``f64_plain`` / ``other_paths`` -- the plain FP64 kernel (on a slab) and
+                the mixed-precision pointwise kernel on the same workload;
 * ``cpu_baseline`` -- the FP64 C/OpenMP oracle on a bounded slab of the same
                 grid, all host cores;
 * ``--impl reference`` -- the same oracle as the reference arm (the
@@ -47,6 +50,9 @@ GRID = 256
 N_MODES = 2000
 VAR = 2.0
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
+# DRAM bytes (read + write) of one contraction launch on this workload, from
+# the ncu capture summarised in profiles/grid_tc_kernel_exp3d_grid256.md.
+TC_DRAM_BYTES_PER_LAUNCH = 34.4e6
 
 
 def parse():
@@ -198,6 +204,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def tensor_peak():
+    """Measured dense bf16 tensor peak (TFLOP/s) and where it came from."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
 def run_ours(args):
     import torch
 
@@ -212,7 +228,7 @@ def run_ours(args):
 
         dist.init_process_group("nccl", device_id=dev)
     build.build()
-    lib = _native.load()
+    _native.load()
 
     cov, z1, z2 = load_modes()
     n = args.grid
@@ -220,6 +236,7 @@ def run_ours(args):
     n_pts = n ** 3
     work = N_MODES * n_pts
     scale = float(np.sqrt(VAR / N_MODES))
+    path = "tensor" if args.path == "auto" else args.path
 
     d_cov = torch.from_numpy(np.ascontiguousarray(cov)).to(dev)
     d_z1 = torch.from_numpy(z1).to(dev)
@@ -230,39 +247,19 @@ def run_ours(args):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
+    ws_bytes = ctypes.c_size_t(0)
+    _native.call("gst_grid_tc_workspace_size", 3, N_MODES, lens,
+                 ctypes.byref(ws_bytes))
+    ws = torch.empty(max(ws_bytes.value, 1), dtype=torch.uint8, device=dev)
 
     def p(t):
         return ctypes.c_void_p(t.data_ptr())
-
-    def step_mixed():
-        _native.call("gst_summate_grid_mixed", 3, N_MODES, lens, p(d_axes),
-                     p(d_cov), p(d_z1), p(d_z2), p(out32), _native.GST_OUT_F32,
-                     scale, sp)
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
 
             dist.barrier()
-
-    def timed(fn, steps, warmup):
-        for _ in range(warmup):
-            fn()
-        torch.cuda.synchronize()
-        barrier()
-        times = []
-        for _ in range(steps):
-            flush.fill_(1.0)
-            ev0 = torch.cuda.Event(enable_timing=True)
-            ev1 = torch.cuda.Event(enable_timing=True)
-            ev0.record(stream)
-            fn()
-            ev1.record(stream)
-            ev1.synchronize()
-            times.append(ev0.elapsed_time(ev1) / 1e3)
-        torch.cuda.synchronize()
-        barrier()
-        return times
 
     def max_over_ranks(x):
         if world == 1:
@@ -273,26 +270,80 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    # -- headline path: mixed-precision grid kernel -----------------------
+    def tc_tables():
+        _native.call("gst_grid_tc_tables", 3, N_MODES, lens, p(d_axes),
+                     p(d_cov), p(d_z1), p(d_z2), p(ws), ws_bytes, sp)
+
+    def tc_contract():
+        _native.call("gst_grid_tc_contract", 3, N_MODES, lens, p(ws),
+                     ws_bytes, p(out32), _native.GST_OUT_F32, scale, sp)
+
+    def step_mixed():
+        _native.call("gst_summate_grid_mixed", 3, N_MODES, lens, p(d_axes),
+                     p(d_cov), p(d_z1), p(d_z2), p(out32), _native.GST_OUT_F32,
+                     scale, sp)
+
+    if path == "tensor":
+        parts = [tc_tables, tc_contract]
+        launches_per_step = 2
+        desc = "separable 3xTF32 tensor-core grid path (tables + contraction)"
+    else:
+        parts = [step_mixed]
+        launches_per_step = 2
+        desc = "mixed-precision pointwise grid kernel"
+
+    def timed(parts, steps, warmup):
+        """Per step: L2 flush, then events around each part."""
+        for _ in range(warmup):
+            for fn in parts:
+                fn()
+        torch.cuda.synchronize()
+        barrier()
+        per_part = [[] for _ in parts]
+        totals = []
+        for _ in range(steps):
+            flush.fill_(1.0)
+            evs = [torch.cuda.Event(enable_timing=True)
+                   for _ in range(len(parts) + 1)]
+            evs[0].record(stream)
+            for i, fn in enumerate(parts):
+                fn()
+                evs[i + 1].record(stream)
+            evs[-1].synchronize()
+            for i in range(len(parts)):
+                per_part[i].append(evs[i].elapsed_time(evs[i + 1]) / 1e3)
+            totals.append(evs[0].elapsed_time(evs[-1]) / 1e3)
+        torch.cuda.synchronize()
+        barrier()
+        return totals, per_part
+
+    # -- headline ----------------------------------------------------------
     clocks = Clocks(local)
     clocks.start()
-    times = timed(step_mixed, args.steps, args.warmup)
+    totals, per_part = timed(parts, args.steps, args.warmup)
     clk = clocks.stop()
-    t_step = max_over_ranks(statistics.mean(times))
+    t_step = max_over_ranks(statistics.mean(totals))
     value = world * work / t_step / 1e9
+    t_main = max_over_ranks(statistics.mean(per_part[-1]))
 
-    # -- error of the headline path vs the FP64 kernel on a sub-block -----
-    sub = [a[:: max(1, n // 32)] for a in axes]
+    # -- error of the headline output vs the FP64 kernel on a sub-grid ------
+    stride = max(1, n // 32)
+    sub = [a[::stride] for a in axes]
     ref64 = gg.summate_grid(cov, z1, z2, sub, scale=scale)
-    got = gg.summate_grid(cov, z1, z2, sub, precision="mixed",
-                          out_dtype="float32", scale=scale)
-    diff = got.astype(np.float64) - ref64
+    got = out32[::stride, ::stride, ::stride].double().cpu().numpy()
+    diff = got - ref64
     sigma = np.sqrt(VAR)
-    err = {"max_abs_sigma": float(np.max(np.abs(diff)) / sigma),
-           "rms_sigma": float(np.sqrt(np.mean(diff**2)) / sigma),
-           "vs": "FP64 grid kernel", "points": int(diff.size)}
+    err = {"rms_sigma": float(np.sqrt(np.mean(diff**2)) / sigma),
+           "max_abs_sigma": float(np.max(np.abs(diff)) / sigma),
+           "vs": "FP64 grid kernel (reference op order)",
+           "points": int(diff.size)}
 
-    # -- plain FP64 kernel on a slab of the same grid ---------------------
+    # -- the other paths, for the record ------------------------------------
+    others = {}
+    if path == "tensor":
+        t_mx, _ = timed([step_mixed], 3, 1)
+        others["mixed_pointwise"] = world * work / max_over_ranks(
+            statistics.mean(t_mx)) / 1e9
     slab = max(1, n // 16)
     lens64 = (ctypes.c_int64 * 4)(slab, n, n, 1)
     out64 = torch.empty((slab, n, n), dtype=torch.float64, device=dev)
@@ -301,17 +352,20 @@ def run_ours(args):
         _native.call("gst_summate_grid_f64", 3, N_MODES, lens64, p(d_axes),
                      p(d_cov), p(d_z1), p(d_z2), p(out64), sp)
 
-    t64 = timed(step_f64, 2, 1)
+    t64, _ = timed([step_f64], 2, 1)
     f64_value = world * N_MODES * slab * n * n / max_over_ranks(
         statistics.mean(t64)) / 1e9
 
     # -- end to end through the public API (host arrays in and out) --------
+    method = "tensor" if path == "tensor" else "pointwise"
+
     def step_e2e():
         return gg.summate_grid(cov, z1, z2, axes, precision="mixed",
-                               out_dtype="float32", scale=scale)
+                               method=method, out_dtype="float32",
+                               scale=scale)
 
     for _ in range(2):
-        step_e2e()
+        res = step_e2e()
     torch.cuda.synchronize()
     barrier()
     e2e_times = []
@@ -325,7 +379,7 @@ def run_ours(args):
     h2d = cov.nbytes + z1.nbytes + z2.nbytes + sum(a.nbytes for a in axes)
     d2h = res.nbytes
 
-    # -- roofline: FP32 pipe of the mixed kernel, measured peak ------------
+    # -- roofline of the dominant kernel -------------------------------------
     sink = torch.zeros(256, dtype=torch.float32, device=dev)
     ops = ctypes.c_double(0.0)
 
@@ -342,11 +396,33 @@ def run_ours(args):
             best = max(best, ops.value / (ev0.elapsed_time(ev1) / 1e3))
         return best
 
-    peak_f32 = probe(0, 4096) / 1e12
-    peak_f64 = probe(1, 64) / 1e12
-    peak_sfu = probe(2, 512) / 1e12
-    flops_per_mp = 2 * 3 + 4  # phase FMAs + accumulation (algorithmic)
-    achieved = work * flops_per_mp / t_step / 1e12
+    peaks = {"fp32_tflops": probe(0, 4096) / 1e12,
+             "fp64_tflops": probe(1, 64) / 1e12,
+             "sfu_tops": probe(2, 512) / 1e12}
+    if path == "tensor":
+        peak, peak_src = tensor_peak()
+        alg = 4.0 * work / t_main / 1e12
+        n_pad = -(-N_MODES // 8) * 8
+        executed = 12.0 * n_pad * (-(-n // 128) * 128) * n * n / t_main / 1e12
+        roof = {"bound": "tensor", "achieved": alg, "peak": peak,
+                "unit": "TFLOP/s", "frac": alg / peak,
+                "traffic": TC_DRAM_BYTES_PER_LAUNCH,
+                "traffic_note": ("dram read+write bytes per contraction "
+                                 "launch (ncu); the 67 MB float32 field "
+                                 "stays in L2 at launch end"),
+                "kernel": "grid_tc_kernel (contraction)",
+                "kernel_ms": t_main * 1e3,
+                "note": (f"achieved = 4 algorithmic flops per mode*point "
+                         f"(Re of a complex MAC) / contraction time; peak = "
+                         f"{peak_src} dense bf16; the kernel executes "
+                         f"{executed:.0f} TFLOP/s of TF32 MMAs (3xTF32 "
+                         f"split, padded), TF32 runs at half the bf16 rate")}
+    else:
+        alg = 10.0 * work / t_main / 1e12
+        roof = {"bound": "fp32", "achieved": alg, "peak": peaks["fp32_tflops"],
+                "unit": "TFLOP/s", "frac": alg / peaks["fp32_tflops"],
+                "traffic": None, "kernel": "pointwise_kernel (mixed)",
+                "note": "10 algorithmic flops per mode*point vs measured FP32"}
 
     line = {
         "metric": METRIC,
@@ -359,14 +435,15 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32+exact-turn-reduction (sincos SFU, FP64 block sums)",
+        "dtype": ("tf32x3 (fp32 accumulate)" if path == "tensor"
+                  else "fp32 + exact turn reduction"),
         "data": "synthetic (modes from the reference RNG, fixture)",
         "config": {
             "workload": f"exp3d_grid{n}_modes{N_MODES}",
             "model": "Exponential(dim=3, var=2, len_scale=[20,10,5])",
             "grid": [n, n, n], "modes": N_MODES,
             "mode_points_per_step": work,
-            "path": "mixed pointwise grid kernel",
+            "path": desc,
             "output": "float32, scaled by sqrt(var/N)",
             "l2": "512 MB buffer written between timed steps",
             "parallelism": f"replicas x{world}",
@@ -374,19 +451,15 @@ def run_ours(args):
         "error_vs_fp64": err,
         "f64_plain": {"value": f64_value, "unit": UNIT,
                       "sample": f"{slab}x{n}x{n} slab, FP64 grid kernel",
-                      "speedup_of_value": value / f64_value},
+                      "value_over_f64": value / f64_value},
+        "other_paths": others,
         "e2e": {"value": world * work / e2e_t / 1e9, "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_f32,
-                     "unit": "TFLOP/s", "frac": achieved / peak_f32,
-                     "traffic": None,
-                     "note": ("algorithmic 10 flops/mode*point; peak = "
-                              "measured FP32 FMA probe on this GPU")},
-        "measured_peaks": {"fp32_tflops": peak_f32, "fp64_tflops": peak_f64,
-                           "sfu_tops": peak_sfu},
+        "roofline": roof,
+        "measured_peaks": peaks,
         "clocks": clk,
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches_per_step * args.steps,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cov, z1, z2, axes)

@@ -56,6 +56,13 @@ SIGNATURES = {
                                                 _dbl, _ptr]),
     "gst_summate_grid_tc": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr, _ptr,
                                      _ptr, _ptr, _c_int, _dbl, _ptr]),
+    "gst_grid_tc_workspace_size": (_c_int, [_c_int, _i64, _ptr,
+                                            ctypes.POINTER(ctypes.c_size_t)]),
+    "gst_grid_tc_tables": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr, _ptr,
+                                    _ptr, _ptr, ctypes.c_size_t, _ptr]),
+    "gst_grid_tc_contract": (_c_int, [_c_int, _i64, _ptr, _ptr,
+                                      ctypes.c_size_t, _ptr, _c_int, _dbl,
+                                      _ptr]),
     "gst_peak_probe": (_c_int, [_c_int, _i64, _ptr, ctypes.POINTER(_dbl),
                                 _ptr]),
 }

@@ -104,20 +104,30 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
 // for completes within microseconds when the hardware is healthy.
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Waits for `parity` of `bar`; gives up after kWaitLimitNs, records the
-// timeout in *err and returns false.
+// timeout in *err and returns false.  try_wait suspends the thread in
+// hardware between checks, so waiting warps do not steal issue slots.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
                                           unsigned int *err) {
-    if (mbar_test(bar, parity)) return true;
+    if (mbar_try(bar, parity)) return true;
     const uint64_t t0 = global_timer_ns();
     for (uint32_t it = 1;; ++it) {
-        if (mbar_test(bar, parity)) return true;
-        if ((it & 63u) == 0u) {
-            if (global_timer_ns() - t0 > kWaitLimitNs) {
-                atomicOr(err, kErrWaitTimeout);
-                return false;
-            }
-            __nanosleep(32);
+        if (mbar_try(bar, parity)) return true;
+        if ((it & 15u) == 0u && global_timer_ns() - t0 > kWaitLimitNs) {
+            atomicOr(err, kErrWaitTimeout);
+            return false;
         }
     }
 }

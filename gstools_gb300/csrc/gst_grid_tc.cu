@@ -27,12 +27,12 @@
 // points, 320 threads):
 //   warp 0      bulk-copy (TMA) producer: per stage the pre-split A image
 //               (16 KB, already in the UMMA canonical K-major layout) and the
-//               stage's Ey / Ez table slices;
+//               stage's Ey / Ez table slices, into a 6-deep ring;
 //   warp 1      allocates 512 TMEM columns (two 128 x 256 FP32 accumulators)
 //               and issues tcgen05.mma from one thread, M=128 N=256 K=8,
 //               3 MMAs per K-step;
-//   warps 2-9   generate B = Ey * Ez (complex product, TF32 split) into the
-//               stage's shared memory, drain finished chunk accumulators
+//   warps 2-9   generate B = Ey * Ez (complex product, TF32 split) into a
+//               3-deep ring of B slots, drain finished chunk accumulators
 //               into registers (tcgen05.ld), and store the scaled tile.
 // Every mbarrier wait is bounded (gst::mbar_wait); a timeout is recorded in
 // the device error word and the CTA still frees its tensor memory.
@@ -265,6 +265,10 @@ struct GridArgs {
     unsigned int *err;
 };
 
+// Shared memory: a ring of bulk-copied slots (A image + Ey / Ez slices) and a
+// ring of generated B slots.  The copy ring is deeper so the bulk copies are
+// issued several stages ahead of the tensor cores; the B ring only has to
+// cover the generation time.
 template <int TY>
 struct StageLayout {
     static constexpr int TZ = kTileCols / TY;
@@ -273,11 +277,17 @@ struct StageLayout {
     static constexpr int kA = 0;
     static constexpr int kEy = kA + kAStageBytes;
     static constexpr int kEz = kEy + kEyBytes;
-    static constexpr int kB = (kEz + kEzBytes + 1023) / 1024 * 1024;
-    static constexpr int kBytes = kB + kBStageBytes;
     static constexpr int kCopyBytes = kAStageBytes + kEyBytes + kEzBytes;
-    static constexpr int kPipe = (4 * kBytes + 2048 <= 227 * 1024) ? 4 : 3;
-    static constexpr int kSmem = kPipe * kBytes + 1024 /*align*/ + 256 /*bars*/;
+    static constexpr int kSlotA = (kCopyBytes + 1023) / 1024 * 1024;
+    static constexpr int kSlotB = kBStageBytes;
+    static constexpr int kPipeB = 3;
+    static constexpr int kBudget = 227 * 1024 - 2048;
+    static constexpr int kPipeA0 = (kBudget - kPipeB * kSlotB) / kSlotA;
+    static constexpr int kPipeA = kPipeA0 > 6 ? 6 : kPipeA0;
+    static constexpr int kRingB = kPipeA * kSlotA;
+    static constexpr int kBars = kRingB + kPipeB * kSlotB;
+    static constexpr int kSmem = kBars + 1024 /*align*/ + 256 /*bars*/;
+    static_assert(kPipeA >= 3, "copy ring too shallow");
 };
 
 template <int TY>
@@ -285,18 +295,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     grid_tc_kernel(const GridArgs a) {
     using L = StageLayout<TY>;
     constexpr int TZ = L::TZ;
-    constexpr int P = L::kPipe;
+    constexpr int PA = L::kPipeA;
+    constexpr int PB = L::kPipeB;
 
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + P * L::kBytes);
-    uint64_t *full = bars;           // [P] bulk copies landed
-    uint64_t *bready = bars + P;     // [P] B generated
-    uint64_t *empty = bars + 2 * P;  // [P] MMAs done with the stage
-    uint64_t *chunk_done = bars + 3 * P;     // [2] accumulator b complete
-    uint64_t *acc_free = bars + 3 * P + 2;   // [2] accumulator b drained
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 3 * P + 4);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::kBars);
+    uint64_t *full = bars;                 // [PA] bulk copies landed
+    uint64_t *empty = bars + PA;           // [PA] MMAs done with copy slot
+    uint64_t *bready = bars + 2 * PA;      // [PB] B generated
+    uint64_t *bfree = bars + 2 * PA + PB;  // [PB] MMAs done with B slot
+    uint64_t *chunk_done = bars + 2 * PA + 2 * PB;  // [2] accumulator done
+    uint64_t *acc_free = chunk_done + 2;            // [2] accumulator drained
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_free + 2);
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -310,10 +322,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int64_t n_chunks = ceil_div_dev(n_st, kChunkStages);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < P; ++s) {
+        for (int s = 0; s < PA; ++s) {
             mbar_init(&full[s], 1);
-            mbar_init(&bready[s], kGenThreads / 32);
             mbar_init(&empty[s], 1);
+        }
+        for (int s = 0; s < PB; ++s) {
+            mbar_init(&bready[s], kGenThreads / 32);
+            mbar_init(&bfree[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&chunk_done[b], 1);
@@ -335,11 +350,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             const float2 *ey_src = a.ey + yb * n_st * kModesPerStage * TY;
             const float2 *ez_src = a.ez + zb * n_st * kModesPerStage * TZ;
             for (int64_t st = 0; st < n_st && ok; ++st) {
-                const int s = static_cast<int>(st % P);
-                const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
+                const int s = static_cast<int>(st % PA);
+                const uint32_t ph = static_cast<uint32_t>((st / PA) & 1);
                 ok = mbar_wait(&empty[s], ph ^ 1u, a.err);
                 if (!ok) break;
-                unsigned char *dst = smem + s * L::kBytes;
+                unsigned char *dst = smem + s * L::kSlotA;
                 mbar_arrive_expect_tx(&full[s], L::kCopyBytes);
                 bulk_copy_g2s(dst + L::kA, a_src + st * kAStageBytes,
                               kAStageBytes, &full[s]);
@@ -353,8 +368,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ---------------------------------------------- MMA issuer --
         if (lane == 0) {
             for (int64_t st = 0; st < n_st && ok; ++st) {
-                const int s = static_cast<int>(st % P);
-                const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
+                const int sa = static_cast<int>(st % PA);
+                const uint32_t pha = static_cast<uint32_t>((st / PA) & 1);
+                const int sb = static_cast<int>(st % PB);
+                const uint32_t phb = static_cast<uint32_t>((st / PB) & 1);
                 const int64_t c = st / kChunkStages;
                 const int buf = static_cast<int>(c & 1);
                 const bool first = (st % kChunkStages) == 0;
@@ -364,17 +381,18 @@ __global__ void __launch_bounds__(kThreads, 1)
                                    static_cast<uint32_t>(((c >> 1) - 1) & 1), a.err);
                     if (!ok) break;
                 }
-                ok = mbar_wait(&full[s], ph, a.err) &&
-                     mbar_wait(&bready[s], ph, a.err);
+                ok = mbar_wait(&full[sa], pha, a.err) &&
+                     mbar_wait(&bready[sb], phb, a.err);
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t base = smem_addr(smem + s * L::kBytes);
+                const uint32_t abase = smem_addr(smem + sa * L::kSlotA + L::kA);
+                const uint32_t bbase = smem_addr(smem + L::kRingB + sb * L::kSlotB);
                 const uint32_t d = tmem + buf * 256;
 #pragma unroll
                 for (int ks = 0; ks < kKSteps; ++ks) {
-                    const uint64_t bh = smem_desc(base + L::kB + (ks * 2 + 0) * kBBlockBytes);
-                    const uint64_t bl = smem_desc(base + L::kB + (ks * 2 + 1) * kBBlockBytes);
-                    const uint32_t ablk = base + L::kA + ks * 2 * kABlockBytes;
+                    const uint64_t bh = smem_desc(bbase + (ks * 2 + 0) * kBBlockBytes);
+                    const uint64_t bl = smem_desc(bbase + (ks * 2 + 1) * kBBlockBytes);
+                    const uint32_t ablk = abase + ks * 2 * kABlockBytes;
                     const uint64_t ah = smem_desc(ablk);
                     const uint64_t al = smem_desc(ablk + kABlockBytes);
                     const uint32_t acc = (first && ks == 0) ? 0u : 1u;
@@ -382,7 +400,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     mma_tf32(d, ah, bl, 1u);
                     mma_tf32(d, al, bh, 1u);
                 }
-                mma_commit(&empty[s]);
+                mma_commit(&empty[sa]);
+                mma_commit(&bfree[sb]);
                 if ((st % kChunkStages) == kChunkStages - 1 || st == n_st - 1)
                     mma_commit(&chunk_done[buf]);
             }
@@ -423,13 +442,17 @@ __global__ void __launch_bounds__(kThreads, 1)
         };
 
         for (int64_t st = 0; st < n_st && ok; ++st) {
-            const int s = static_cast<int>(st % P);
-            const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
-            ok = mbar_wait(&full[s], ph, a.err);
+            const int sa = static_cast<int>(st % PA);
+            const uint32_t pha = static_cast<uint32_t>((st / PA) & 1);
+            const int sb = static_cast<int>(st % PB);
+            const uint32_t phb = static_cast<uint32_t>((st / PB) & 1);
+            ok = mbar_wait(&bfree[sb], phb ^ 1u, a.err) &&
+                 mbar_wait(&full[sa], pha, a.err);
             if (__any_sync(0xffffffffu, !ok)) { ok = false; break; }
-            unsigned char *stage = smem + s * L::kBytes;
-            const float2 *sey = reinterpret_cast<const float2 *>(stage + L::kEy);
-            const float2 *sez = reinterpret_cast<const float2 *>(stage + L::kEz);
+            const unsigned char *slot = smem + sa * L::kSlotA;
+            const float2 *sey = reinterpret_cast<const float2 *>(slot + L::kEy);
+            const float2 *sez = reinterpret_cast<const float2 *>(slot + L::kEz);
+            unsigned char *bslot = smem + L::kRingB + sb * L::kSlotB;
 #pragma unroll
             for (int ks = 0; ks < kKSteps; ++ks) {
                 float hi[8], lo[8];
@@ -445,8 +468,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     hi[2 * m + 1] = to_tf32(im);
                     lo[2 * m + 1] = to_tf32(im - hi[2 * m + 1]);
                 }
-                unsigned char *bh = stage + L::kB + (ks * 2 + 0) * kBBlockBytes;
-                unsigned char *bl = stage + L::kB + (ks * 2 + 1) * kBBlockBytes;
+                unsigned char *bh = bslot + (ks * 2 + 0) * kBBlockBytes;
+                unsigned char *bl = bslot + (ks * 2 + 1) * kBBlockBytes;
 #pragma unroll
                 for (int kb = 0; kb < 2; ++kb) {
                     const uint32_t o = core_offset(gt, kb * 4);
@@ -458,11 +481,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             fence_async_smem();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&bready[s]);
-            // Drain the previous chunk once the MMAs are past it: the
-            // generators run at most P stages ahead of the tensor cores.
+            if (lane == 0) mbar_arrive(&bready[sb]);
+            // Drain the previous chunk once the MMAs are past it: generating
+            // stage st needed the MMAs of stage st - PB to be complete.
             if (drained < n_chunks - 1 &&
-                st == (drained + 1) * kChunkStages - 1 + (P - 1)) {
+                st == (drained + 1) * kChunkStages - 1 + PB) {
                 ok = drain(drained);
                 ++drained;
             }
@@ -514,17 +537,21 @@ cudaError_t launch_grid(const GridArgs &args, int64_t n_tiles, cudaStream_t s) {
 }  // namespace
 }  // namespace gst
 
-extern "C" int gst_summate_grid_tc(int dim, int64_t n_modes,
-                                   const int64_t *axis_len, const double *axes,
-                                   const double *cov_samples, const double *z_1,
-                                   const double *z_2, void *out, int out_type,
-                                   double scale, void *stream) {
-    using namespace gst;
+namespace gst {
+namespace {
+
+struct GridPlan {
+    GridGeom g;
+    int ty, tz;
+    size_t a_bytes, ey_off, ez_off, total;
+};
+
+int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
+              int64_t &total_pts) {
     if (dim < 2 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
     if (axis_len == nullptr || n_modes < 0) return GST_ERR_INVALID_ARGUMENT;
-    if (out_type != GST_OUT_F64 && out_type != GST_OUT_F32)
-        return GST_ERR_INVALID_ARGUMENT;
-    GridGeom g{};
+    GridGeom &g = p.g;
+    g = GridGeom{};
     int64_t total = 1, off = 0;
     for (int d = 0; d < 3; ++d) {
         g.n[d] = d < dim ? axis_len[d] : 1;
@@ -533,66 +560,156 @@ extern "C" int gst_summate_grid_tc(int dim, int64_t n_modes,
         off += d < dim ? g.n[d] : 0;
         total *= g.n[d];
     }
+    total_pts = total;
+    p.ty = dim == 3 ? 16 : kTileCols;
+    p.tz = kTileCols / p.ty;
+    g.tile[0] = kXBlock;
+    g.tile[1] = p.ty;
+    g.tile[2] = p.tz;
+    for (int d = 0; d < 3; ++d) g.blocks[d] = ceil_div(g.n[d], g.tile[d]);
+    g.n_stages = ceil_div(n_modes, kModesPerStage);
+    g.n_modes = n_modes;
+    if (g.blocks[0] * g.blocks[1] * g.blocks[2] > 0x7fffffffLL)
+        return GST_ERR_TOO_LARGE;
+    p.a_bytes = static_cast<size_t>(g.blocks[0]) * g.n_stages * kAStageBytes;
+    const size_t ey_bytes = static_cast<size_t>(g.blocks[1]) * g.n_stages *
+                            kModesPerStage * p.ty * sizeof(float2);
+    const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages *
+                            kModesPerStage * p.tz * sizeof(float2);
+    p.ey_off = align_up(p.a_bytes, 256);
+    p.ez_off = align_up(p.ey_off + ey_bytes, 256);
+    p.total = p.ez_off + ez_bytes;
+    return GST_OK;
+}
+
+int run_tables(const GridPlan &p, int dim, const double *axes,
+               const double *cov, const double *z1, const double *z2,
+               unsigned char *ws, cudaStream_t s) {
+    const GridGeom &g = p.g;
+    const int64_t n_pad_modes = g.n_stages * kModesPerStage;
+    int64_t max_rows = 0;
+    for (int d = 0; d < 3; ++d)
+        max_rows = std::max(max_rows, g.blocks[d] * g.tile[d]);
+    const int threads = 256;
+    const dim3 grid(static_cast<unsigned>(ceil_div(max_rows * n_pad_modes, threads)),
+                    1, 3);
+    grid_tables_kernel<<<grid, threads, 0, s>>>(
+        g, dim, cov, z1, z2, axes, ws, reinterpret_cast<float2 *>(ws + p.ey_off),
+        reinterpret_cast<float2 *>(ws + p.ez_off));
+    GST_TRY_CUDA(cudaGetLastError());
+    return GST_OK;
+}
+
+int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
+                 int out_type, double scale, cudaStream_t s) {
+    unsigned int *err = device_error_word();
+    if (err == nullptr) return GST_ERR_CUDA;
+    GridArgs args{};
+    args.g = p.g;
+    args.a_image = ws;
+    args.ey = reinterpret_cast<const float2 *>(ws + p.ey_off);
+    args.ez = reinterpret_cast<const float2 *>(ws + p.ez_off);
+    args.out = out;
+    args.out_f32 = out_type == GST_OUT_F32 ? 1 : 0;
+    args.scale = scale;
+    args.err = err;
+    const int64_t n_tiles = p.g.blocks[0] * p.g.blocks[1] * p.g.blocks[2];
+    const cudaError_t e = (p.ty == 16) ? launch_grid<16>(args, n_tiles, s)
+                                       : launch_grid<kTileCols>(args, n_tiles, s);
+    GST_TRY_CUDA(e);
+    return GST_OK;
+}
+
+bool valid_out(int t) { return t == GST_OUT_F64 || t == GST_OUT_F32; }
+
+}  // namespace
+}  // namespace gst
+
+extern "C" {
+
+int gst_grid_tc_workspace_size(int dim, int64_t n_modes,
+                               const int64_t *axis_len, size_t *bytes) {
+    if (bytes == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    gst::GridPlan p;
+    int64_t total = 0;
+    const int rc = gst::make_plan(dim, n_modes, axis_len, p, total);
+    if (rc) return rc;
+    *bytes = (total == 0 || n_modes == 0) ? 0 : p.total;
+    return GST_OK;
+}
+
+int gst_grid_tc_tables(int dim, int64_t n_modes, const int64_t *axis_len,
+                       const double *axes, const double *cov_samples,
+                       const double *z_1, const double *z_2, void *workspace,
+                       size_t workspace_bytes, void *stream) {
+    gst::GridPlan p;
+    int64_t total = 0;
+    int rc = gst::make_plan(dim, n_modes, axis_len, p, total);
+    if (rc) return rc;
+    if (total == 0 || n_modes == 0) return GST_OK;
+    if (workspace == nullptr || workspace_bytes < p.total || axes == nullptr ||
+        cov_samples == nullptr || z_1 == nullptr || z_2 == nullptr)
+        return GST_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+        return GST_ERR_ALIGNMENT;
+    if (gst::current_device() < 0) return GST_ERR_NO_DEVICE;
+    return gst::run_tables(p, dim, axes, cov_samples, z_1, z_2,
+                           static_cast<unsigned char *>(workspace),
+                           static_cast<cudaStream_t>(stream));
+}
+
+int gst_grid_tc_contract(int dim, int64_t n_modes, const int64_t *axis_len,
+                         const void *workspace, size_t workspace_bytes,
+                         void *out, int out_type, double scale, void *stream) {
+    if (!gst::valid_out(out_type)) return GST_ERR_INVALID_ARGUMENT;
+    gst::GridPlan p;
+    int64_t total = 0;
+    int rc = gst::make_plan(dim, n_modes, axis_len, p, total);
+    if (rc) return rc;
     if (total == 0) return GST_OK;
     if (out == nullptr) return GST_ERR_INVALID_ARGUMENT;
-    if (current_device() < 0) return GST_ERR_NO_DEVICE;
+    if (gst::current_device() < 0) return GST_ERR_NO_DEVICE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const size_t elem = out_type == GST_OUT_F32 ? 4 : 8;
     if (n_modes == 0) {
+        const size_t elem = out_type == GST_OUT_F32 ? 4 : 8;
+        GST_TRY_CUDA(cudaMemsetAsync(out, 0, elem * total, s));
+        return GST_OK;
+    }
+    if (workspace == nullptr || workspace_bytes < p.total)
+        return GST_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+        return GST_ERR_ALIGNMENT;
+    return gst::run_contract(p, static_cast<const unsigned char *>(workspace),
+                             out, out_type, scale, s);
+}
+
+int gst_summate_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,
+                        const double *axes, const double *cov_samples,
+                        const double *z_1, const double *z_2, void *out,
+                        int out_type, double scale, void *stream) {
+    if (!gst::valid_out(out_type)) return GST_ERR_INVALID_ARGUMENT;
+    gst::GridPlan p;
+    int64_t total = 0;
+    int rc = gst::make_plan(dim, n_modes, axis_len, p, total);
+    if (rc) return rc;
+    if (total == 0) return GST_OK;
+    if (out == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    if (gst::current_device() < 0) return GST_ERR_NO_DEVICE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (n_modes == 0) {
+        const size_t elem = out_type == GST_OUT_F32 ? 4 : 8;
         GST_TRY_CUDA(cudaMemsetAsync(out, 0, elem * total, s));
         return GST_OK;
     }
     if (cov_samples == nullptr || z_1 == nullptr || z_2 == nullptr ||
         axes == nullptr)
         return GST_ERR_INVALID_ARGUMENT;
-
-    const int ty = dim == 3 ? 16 : kTileCols;
-    const int tz = kTileCols / ty;
-    g.tile[0] = kXBlock;
-    g.tile[1] = ty;
-    g.tile[2] = tz;
-    for (int d = 0; d < 3; ++d) g.blocks[d] = ceil_div(g.n[d], g.tile[d]);
-    g.n_stages = ceil_div(n_modes, kModesPerStage);
-    g.n_modes = n_modes;
-    const int64_t n_tiles = g.blocks[0] * g.blocks[1] * g.blocks[2];
-    if (n_tiles > 0x7fffffffLL) return GST_ERR_TOO_LARGE;
-
-    const size_t a_bytes = static_cast<size_t>(g.blocks[0]) * g.n_stages * kAStageBytes;
-    const size_t ey_bytes = static_cast<size_t>(g.blocks[1]) * g.n_stages *
-                            kModesPerStage * ty * sizeof(float2);
-    const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages *
-                            kModesPerStage * tz * sizeof(float2);
-    const size_t ey_off = align_up(a_bytes, 256);
-    const size_t ez_off = align_up(ey_off + ey_bytes, 256);
-    unsigned int *err = device_error_word();
-    if (err == nullptr) return GST_ERR_CUDA;
-
-    StreamScratch ws;
-    GST_TRY_CUDA(ws.alloc(ez_off + ez_bytes, s));
+    gst::StreamScratch ws;
+    GST_TRY_CUDA(ws.alloc(p.total, s));
     unsigned char *base = static_cast<unsigned char *>(ws.ptr);
-
-    const int64_t n_pad_modes = g.n_stages * kModesPerStage;
-    int64_t max_rows = 0;
-    for (int d = 0; d < 3; ++d) max_rows = std::max(max_rows, g.blocks[d] * g.tile[d]);
-    const int threads = 256;
-    const dim3 tgrid(static_cast<unsigned>(ceil_div(max_rows * n_pad_modes, threads)), 1, 3);
-    grid_tables_kernel<<<tgrid, threads, 0, s>>>(
-        g, dim, cov_samples, z_1, z_2, axes, base,
-        reinterpret_cast<float2 *>(base + ey_off),
-        reinterpret_cast<float2 *>(base + ez_off));
-    GST_TRY_CUDA(cudaGetLastError());
-
-    GridArgs args{};
-    args.g = g;
-    args.a_image = base;
-    args.ey = reinterpret_cast<const float2 *>(base + ey_off);
-    args.ez = reinterpret_cast<const float2 *>(base + ez_off);
-    args.out = out;
-    args.out_f32 = out_type == GST_OUT_F32 ? 1 : 0;
-    args.scale = scale;
-    args.err = err;
-    const cudaError_t e = (ty == 16) ? launch_grid<16>(args, n_tiles, s)
-                                     : launch_grid<kTileCols>(args, n_tiles, s);
-    GST_TRY_CUDA(e);
-    return GST_OK;
+    rc = gst::run_tables(p, dim, axes, cov_samples, z_1, z_2, base, s);
+    if (rc) return rc;
+    return gst::run_contract(p, base, out, out_type, scale, s);
 }
+
+}  // extern "C"

@@ -38,6 +38,7 @@
 #ifndef GSTOOLS_GB300_H
 #define GSTOOLS_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -173,6 +174,25 @@ int gst_summate_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,
                         const double *axes, const double *cov_samples,
                         const double *z_1, const double *z_2, void *out,
                         int out_type, double scale, void *stream);
+
+/* The tensor-core grid path in two steps with a caller-owned workspace, so
+ * that the per-axis tables can be built once and contracted many times (and
+ * each step timed on its own).  The workspace is device memory, 256-byte
+ * aligned, of at least the size gst_grid_tc_workspace_size reports (0 when
+ * there is nothing to do).  gst_grid_tc_tables fills it from the modes and
+ * axes; gst_grid_tc_contract writes the field from it.  Arguments otherwise
+ * as gst_summate_grid_tc; both calls must see the same dim, n_modes and
+ * axis_len.  No counterpart in the reference (its summation has no
+ * precomputation step). */
+int gst_grid_tc_workspace_size(int dim, int64_t n_modes,
+                               const int64_t *axis_len, size_t *bytes);
+int gst_grid_tc_tables(int dim, int64_t n_modes, const int64_t *axis_len,
+                       const double *axes, const double *cov_samples,
+                       const double *z_1, const double *z_2, void *workspace,
+                       size_t workspace_bytes, void *stream);
+int gst_grid_tc_contract(int dim, int64_t n_modes, const int64_t *axis_len,
+                         const void *workspace, size_t workspace_bytes,
+                         void *out, int out_type, double scale, void *stream);
 
 /* ----------------------------------------------------------------------- */
 /* Diagnostics (no reference counterpart).                                  */
