@@ -37,6 +37,8 @@ SIGNATURES = {
     "gst_read_device_error": (_c_int, [_ptr, ctypes.POINTER(_u32)]),
     "gst_summate_f64": (_c_int, [_c_int, _i64, _i64, _ptr, _ptr, _ptr, _ptr,
                                  _ptr, _ptr]),
+    "gst_summate_f64_noalloc": (_c_int, [_c_int, _i64, _i64, _ptr, _ptr,
+                                         _ptr, _ptr, _ptr, _ptr]),
     "gst_summate_incompr_f64": (_c_int, [_c_int, _i64, _i64, _ptr, _ptr,
                                          _ptr, _ptr, _ptr, _ptr]),
     "gst_summate_fourier_f64": (_c_int, [_c_int, _i64, _i64, _ptr, _ptr,

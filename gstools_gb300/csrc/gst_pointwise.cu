@@ -23,6 +23,7 @@
 //     split across blockIdx.y and a second kernel adds the FP64 partial sums in
 //     a fixed order (deterministic results).
 #include <algorithm>
+#include <mutex>
 
 #include "gst_common.cuh"
 
@@ -695,3 +696,144 @@ int gst_summate_incompr_grid_mixed(int dim, int64_t n_modes,
 }
 
 }  // extern "C"
+
+// ===================================================================
+// Allocation-free FP64 summate.
+//
+// Some callers cannot let a library allocate device memory: hosts that
+// reserve the GPU's memory for their own pool at start-up and forbid other
+// allocations, and latency-critical loops that cannot pay for an
+// allocator call.  gst_summate_f64_noalloc serves them with the FP64
+// pointwise kernel above, taking its scratch (the packed mode table and the
+// split-mode partial sums) from a fixed array in device memory instead of
+// the stream-ordered allocator.
+//
+// * The array is a file-scope __device__ object of kNoAllocScratchBytes
+//   (5 MiB): every GPU that loads this library holds it until the process
+//   exits.  Limits: at most kNoAllocMaxModes modes; the mode range is split
+//   across CTAs only as far as the partial sums fit in the remaining 4 MiB.
+// * Host code cannot use the array's name as a device address.  The first
+//   call on each device (with that device current) looks the address up
+//   with cudaGetSymbolAddress and caches it; make that first call before
+//   any stream capture.
+// * Every call shares the one array, which keeps the previous call's
+//   contents.  Nothing in it has to start at zero (each call overwrites the
+//   table and every partial sum it reads), but calls that overlap on the
+//   GPU (different streams, or different host threads without ordering)
+//   race on it and must be serialised by the caller.
+// ===================================================================
+namespace gst {
+namespace {
+
+constexpr int64_t kNoAllocMaxModes = 16384;
+constexpr size_t kNoAllocTableBytes =
+    static_cast<size_t>(kNoAllocMaxModes) * kEntryBytes;  // 1 MiB
+constexpr size_t kNoAllocPartialBytes = size_t(4) << 20;    // 4 MiB
+constexpr size_t kNoAllocScratchBytes = kNoAllocTableBytes + kNoAllocPartialBytes;
+
+static __device__ __align__(256) unsigned char
+    g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_ptr[kNoAllocMaxDevices];
+
+// Device address of g_noalloc_scratch on the current device (looked up
+// once per device), or an error status.
+int noalloc_scratch(unsigned char **ptr) {
+    const int dev = current_device();
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return GST_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            note_cuda_error(e);
+            return GST_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    *ptr = g_noalloc_ptr[dev];
+    return GST_OK;
+}
+
+int run_noalloc_f64(const Request &r) {
+    if (r.dim < 1 || r.dim > 4) return GST_ERR_UNSUPPORTED_DIM;
+    if (r.n_modes < 0 || r.n_pts < 0) return GST_ERR_INVALID_ARGUMENT;
+    if (r.n_modes > kNoAllocMaxModes) return GST_ERR_TOO_LARGE;
+    if (r.n_pts == 0) return GST_OK;
+    if (r.out == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    if (current_device() < 0) return GST_ERR_NO_DEVICE;
+    if (r.n_modes == 0) {
+        GST_TRY_CUDA(cudaMemsetAsync(r.out, 0, sizeof(double) * r.n_pts, r.stream));
+        return GST_OK;
+    }
+    if (r.cov == nullptr || r.z1 == nullptr || r.z2 == nullptr || r.pos == nullptr)
+        return GST_ERR_INVALID_ARGUMENT;
+
+    unsigned char *scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    unsigned int *err = device_error_word();
+    if (err == nullptr) return GST_ERR_CUDA;
+
+    using T = Tiling<kF64>;
+    const int64_t n_tiles = ceil_div(r.n_modes, T::kTileModes);
+    const int64_t n_padded = n_tiles * T::kTileModes;
+    const int64_t pts_per_cta = static_cast<int64_t>(T::kThreads) * T::kPoints;
+    const int64_t n_pt_tiles = ceil_div(r.n_pts, pts_per_cta);
+    if (n_pt_tiles > 0x7fffffffLL) return GST_ERR_TOO_LARGE;
+
+    const int64_t target = static_cast<int64_t>(sm_count()) * T::kMinBlocks * 2;
+    int64_t n_split = std::min<int64_t>(n_tiles, ceil_div(target, n_pt_tiles));
+    // the partial sums must fit in the fixed partial region
+    const int64_t fit = static_cast<int64_t>(kNoAllocPartialBytes /
+                                             (sizeof(double) * r.n_pts));
+    n_split = std::max<int64_t>(1, std::min(n_split, fit));
+    const int64_t tiles_per_split = ceil_div(n_tiles, n_split);
+    n_split = ceil_div(n_tiles, tiles_per_split);
+
+    unsigned char *table = scratch;
+    double *partial = reinterpret_cast<double *>(scratch + kNoAllocTableBytes);
+    pack<kScalar, kF64>(r, n_padded, table);
+    GST_TRY_CUDA(cudaGetLastError());
+
+    PointwiseArgs args{};
+    args.table = table;
+    args.n_tiles = n_tiles;
+    args.tiles_per_split = tiles_per_split;
+    args.n_pts = r.n_pts;
+    args.pos = r.pos;
+    for (int d = 0; d < 4; ++d) {
+        args.axis_len[d] = 1;
+        args.axis_off[d] = 0;
+    }
+    args.out = n_split > 1 ? static_cast<void *>(partial) : r.out;
+    args.out_f32 = 0;
+    args.partial = n_split > 1 ? 1 : 0;
+    args.scale = 1.0;
+    args.err = err;
+    const dim3 grid(static_cast<unsigned>(n_pt_tiles), static_cast<unsigned>(n_split));
+    GST_TRY_CUDA((dispatch<kScalar, kF64>(kUnstructured, r.dim, grid, args, r.stream)));
+    if (n_split > 1) {
+        const int rt = 256;
+        reduce_partials_kernel<<<static_cast<unsigned>(ceil_div(r.n_pts, rt)), rt, 0,
+                                 r.stream>>>(partial, n_split, r.n_pts, r.out, 0, 1.0);
+        GST_TRY_CUDA(cudaGetLastError());
+    }
+    return GST_OK;
+}
+
+}  // namespace
+}  // namespace gst
+
+extern "C" int gst_summate_f64_noalloc(int dim, int64_t n_modes, int64_t n_pts,
+                                       const double *cov_samples,
+                                       const double *z_1, const double *z_2,
+                                       const double *pos, double *out,
+                                       void *stream) {
+    auto r = gst::make_request(gst::kScalar, gst::kF64, dim, n_modes, n_pts,
+                               cov_samples, z_1, z_2, pos, out, GST_OUT_F64,
+                               stream);
+    return gst::run_noalloc_f64(r);
+}

@@ -102,6 +102,24 @@ int gst_summate_fourier_f64(int dim, int64_t n_modes, int64_t n_pts,
                             const double *z_1, const double *z_2,
                             const double *pos, double *out, void *stream);
 
+/* Allocation-free variant of gst_summate_f64 (same arguments and result).
+ * No counterpart in the reference: it exists for callers that cannot let a
+ * library allocate device memory -- hosts that reserve the GPU's memory for
+ * their own pool and forbid other allocations, and latency-critical loops
+ * that cannot pay for an allocator call.  Its scratch is a fixed 5 MiB
+ * device array inside the library (held on every GPU that loads it until
+ * the process exits); it never calls cudaMalloc or cudaFree.
+ * Limits: n_modes <= 16384 (GST_ERR_TOO_LARGE beyond); the mode range is
+ * split across CTAs only as far as the partial sums fit in 4 MiB, so small
+ * point counts may run with less parallelism.  The first call on a device
+ * looks up the array's device address (make it before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
+int gst_summate_f64_noalloc(int dim, int64_t n_modes, int64_t n_pts,
+                            const double *cov_samples, const double *z_1,
+                            const double *z_2, const double *pos, double *out,
+                            void *stream);
+
 /* ----------------------------------------------------------------------- */
 /* Mixed-precision pointwise kernels (same inputs, FP64 in).                */
 /* The phase is reduced to turns exactly (error-free FP32 splitting of the  */
