@@ -17,6 +17,7 @@ a C ABI, include/gstools_gb300.h); there is no CPU fallback.
 """
 
 from . import config
+from .batched import BatchedSummator
 from .covmodel import CovModel, Exponential, Gaussian, Matern
 from .generator import IncomprRandMeth, RandMeth
 from .hook import install, uninstall
@@ -34,6 +35,7 @@ __version__ = "0.1.0"
 
 __all__ = [
     "config",
+    "BatchedSummator",
     "CovModel",
     "Gaussian",
     "Exponential",

@@ -65,6 +65,17 @@ SIGNATURES = {
     "gst_grid_tc_contract": (_c_int, [_c_int, _i64, _ptr, _ptr,
                                       ctypes.c_size_t, _ptr, _c_int, _dbl,
                                       _ptr]),
+    "gst_batch_workspace_size": (_c_int, [_c_int, _i64, _ptr, _ptr, _c_int,
+                                          ctypes.POINTER(ctypes.c_size_t)]),
+    "gst_batch_prepare": (_c_int, [_c_int, _i64, _ptr, _ptr, _c_int, _ptr,
+                                   ctypes.c_size_t, _ptr]),
+    "gst_batch_run": (_c_int, [_c_int, _i64, _ptr, _ptr, _c_int, _ptr, _ptr,
+                               _ptr, _ptr, _ptr, _ptr, _c_int, _ptr,
+                               ctypes.c_size_t, _ptr]),
+    "gst_summate_vjp_modes_f64": (_c_int, [_c_int, _i64, _i64] + [_ptr] * 9),
+    "gst_summate_vjp_modes_mixed": (_c_int, [_c_int, _i64, _i64] + [_ptr] * 9),
+    "gst_summate_vjp_pos_f64": (_c_int, [_c_int, _i64, _i64] + [_ptr] * 6),
+    "gst_summate_vjp_pos_mixed": (_c_int, [_c_int, _i64, _i64] + [_ptr] * 6),
     "gst_peak_probe": (_c_int, [_c_int, _i64, _ptr, ctypes.POINTER(_dbl),
                                 _ptr]),
 }

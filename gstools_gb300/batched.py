@@ -1,0 +1,209 @@
+"""Ensembles of realizations in one persistent launch.
+
+The reference draws an ensemble by calling ``SRF`` once per seed, each call
+re-sampling the modes on the host and making one native ``summate`` call
+(src/gstools/field/srf.py:109-163; examples/01_random_field/
+01_srf_ensemble.py).  :class:`BatchedSummator` sums a whole ensemble --
+realizations with their own modes, variances and point sets of uneven size --
+in a single persistent kernel over a queue of (realization, point tile) work
+items (``gst_batch_*`` in include/gstools_gb300.h), replayed from a CUDA
+graph.
+
+The tile shape is chosen per ensemble shape by timing the kernel variants on
+the loaded data (:meth:`BatchedSummator.tune`); the choice is cached per shape
+for the process.
+"""
+
+import ctypes
+import hashlib
+import threading
+
+import numpy as np
+import torch
+
+from . import _native
+from .summator import device
+
+__all__ = ["BatchedSummator", "VARIANTS"]
+
+VARIANTS = (0, 1)  # 512 or 1024 points per work tile
+
+_tune_cache = {}
+_tune_lock = threading.Lock()
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr() if t is not None and t.numel() else 0)
+
+
+class BatchedSummator:
+    """Sum an ensemble of realizations on the GPU in one launch.
+
+    Parameters
+    ----------
+    dim : int
+        Spatial dimension (1, 2 or 3).
+    mode_counts, point_counts : sequence of int
+        Modes and evaluation points of every realization.
+    out_dtype : "float32" or "float64"
+        Element type of the output field.
+    graph : bool
+        Replay the run step from a captured CUDA graph.
+    """
+
+    def __init__(self, dim, mode_counts, point_counts, *, out_dtype="float32",
+                 graph=True):
+        if dim not in (1, 2, 3):
+            raise ValueError("dim must be 1, 2 or 3")
+        if len(mode_counts) != len(point_counts):
+            raise ValueError("one mode count and one point count per item")
+        self.dim = int(dim)
+        self.dev = device()
+        self.modes = np.ascontiguousarray(mode_counts, dtype=np.int64)
+        self.points = np.ascontiguousarray(point_counts, dtype=np.int64)
+        if np.any(self.modes < 0) or np.any(self.points < 0):
+            raise ValueError("counts must be non-negative")
+        self.n_items = len(self.modes)
+        self.mode_off = np.concatenate(([0], np.cumsum(self.modes)))
+        self.point_off = np.concatenate(([0], np.cumsum(self.points)))
+        self.total_modes = int(self.mode_off[-1])
+        self.total_points = int(self.point_off[-1])
+        if out_dtype in ("float32", np.float32, torch.float32):
+            self.out_code, tdtype = _native.GST_OUT_F32, torch.float32
+        elif out_dtype in ("float64", np.float64, torch.float64):
+            self.out_code, tdtype = _native.GST_OUT_F64, torch.float64
+        else:
+            raise ValueError(f"unsupported out_dtype {out_dtype!r}")
+        f64 = dict(dtype=torch.float64, device=self.dev)
+        self.cov = torch.zeros((self.dim, self.total_modes), **f64)
+        self.z1 = torch.zeros(self.total_modes, **f64)
+        self.z2 = torch.zeros(self.total_modes, **f64)
+        self.pos = torch.zeros((self.dim, self.total_points), **f64)
+        self.scales = torch.ones(max(self.n_items, 1), **f64)
+        self.out = torch.zeros(self.total_points, dtype=tdtype, device=self.dev)
+        self._modes_c = self.modes.ctypes.data_as(ctypes.c_void_p)
+        self._points_c = self.points.ctypes.data_as(ctypes.c_void_p)
+        self.use_graph = bool(graph)
+        self.variant = None
+        self.workspace = None
+        self.ws_bytes = ctypes.c_size_t(0)
+        self._graph = None
+        self.key = (self.dim, hashlib.sha1(self.modes.tobytes()
+                                           + self.points.tobytes()).hexdigest())
+
+    # -- data -------------------------------------------------------------
+    def load(self, cov_samples, z_1, z_2, pos, scales=None):
+        """Copy one ensemble's inputs (lists of per-realization arrays, the
+        reference's layouts) into the device buffers."""
+        if not (len(cov_samples) == len(z_1) == len(z_2) == len(pos)
+                == self.n_items):
+            raise ValueError("one array per realization expected")
+        cov = np.zeros((self.dim, self.total_modes))
+        zz1 = np.zeros(self.total_modes)
+        zz2 = np.zeros(self.total_modes)
+        xx = np.zeros((self.dim, self.total_points))
+        for r in range(self.n_items):
+            m0, m1 = self.mode_off[r], self.mode_off[r + 1]
+            p0, p1 = self.point_off[r], self.point_off[r + 1]
+            c = np.asarray(cov_samples[r], dtype=np.float64).reshape(self.dim, -1)
+            x = np.asarray(pos[r], dtype=np.float64).reshape(self.dim, -1)
+            if c.shape[1] != m1 - m0 or x.shape[1] != p1 - p0:
+                raise ValueError(f"realization {r}: sizes do not match the plan")
+            cov[:, m0:m1] = c
+            zz1[m0:m1] = np.asarray(z_1[r], dtype=np.float64).reshape(-1)
+            zz2[m0:m1] = np.asarray(z_2[r], dtype=np.float64).reshape(-1)
+            xx[:, p0:p1] = x
+        for dst, src in ((self.cov, cov), (self.z1, zz1), (self.z2, zz2),
+                         (self.pos, xx)):
+            dst.copy_(torch.from_numpy(src).pin_memory(), non_blocking=True)
+        if scales is not None:
+            s = np.asarray(scales, dtype=np.float64).reshape(-1)
+            if s.size != self.n_items:
+                raise ValueError("one scale per realization expected")
+            self.scales[: self.n_items].copy_(torch.from_numpy(s))
+        else:
+            self.scales.fill_(1.0)
+
+    def split(self, out=None):
+        """Per-realization numpy views of a host copy of ``out``."""
+        host = (self.out if out is None else out).cpu().numpy()
+        return [host[self.point_off[r]:self.point_off[r + 1]]
+                for r in range(self.n_items)]
+
+    # -- planning ---------------------------------------------------------
+    def _prepare(self, variant):
+        nbytes = ctypes.c_size_t(0)
+        _native.call("gst_batch_workspace_size", self.dim, self.n_items,
+                     self._modes_c, self._points_c, variant,
+                     ctypes.byref(nbytes))
+        ws = torch.empty(max(nbytes.value, 256), dtype=torch.uint8,
+                         device=self.dev)
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+        _native.call("gst_batch_prepare", self.dim, self.n_items,
+                     self._modes_c, self._points_c, variant, _ptr(ws),
+                     nbytes, stream)
+        return ws, nbytes
+
+    def _launch(self, variant, ws, nbytes):
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+        _native.call("gst_batch_run", self.dim, self.n_items, self._modes_c,
+                     self._points_c, variant, _ptr(self.cov), _ptr(self.z1),
+                     _ptr(self.z2), _ptr(self.pos), _ptr(self.scales),
+                     _ptr(self.out), self.out_code, _ptr(ws), nbytes, stream)
+
+    def tune(self, repeats=3):
+        """Time every tile variant on the loaded data; keep the fastest."""
+        with _tune_lock:
+            cached = _tune_cache.get(self.key)
+        timings = {}
+        if cached is None:
+            for v in VARIANTS:
+                ws, nbytes = self._prepare(v)
+                self._launch(v, ws, nbytes)  # warm-up
+                best = float("inf")
+                for _ in range(repeats):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    self._launch(v, ws, nbytes)
+                    e1.record()
+                    e1.synchronize()
+                    best = min(best, e0.elapsed_time(e1))
+                timings[v] = best
+            cached = min(timings, key=timings.get)
+            with _tune_lock:
+                _tune_cache[self.key] = cached
+        self.variant = cached
+        self.workspace, self.ws_bytes = self._prepare(self.variant)
+        self._graph = None
+        return timings
+
+    def _capture(self):
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            self._launch(self.variant, self.workspace, self.ws_bytes)
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            self._launch(self.variant, self.workspace, self.ws_bytes)
+        self._graph = graph
+
+    # -- execution --------------------------------------------------------
+    def run(self):
+        """Sum the loaded ensemble into ``self.out`` (asynchronous)."""
+        if self.variant is None:
+            self.tune()
+        if self.use_graph:
+            if self._graph is None:
+                self._capture()
+            self._graph.replay()
+        else:
+            self._launch(self.variant, self.workspace, self.ws_bytes)
+        return self.out
+
+    def __call__(self, cov_samples, z_1, z_2, pos, scales=None):
+        """Load, run and return the per-realization fields (numpy)."""
+        self.load(cov_samples, z_1, z_2, pos, scales)
+        self.run()
+        return self.split()

@@ -1,0 +1,264 @@
+// Adjoint (vector-Jacobian product) of the randomization-method sum with
+// respect to the modes.
+//
+// Forward (src/gstools/field/generator.py:193-199):
+//     u_i = sum_j z1_j cos(phi_ij) + z2_j sin(phi_ij),   phi_ij = <k_j, x_i>
+// Given g_i = dL/du_i:
+//     dL/dz1_j   = sum_i g_i cos(phi_ij)
+//     dL/dz2_j   = sum_i g_i sin(phi_ij)
+//     dL/dk_jd   = z2_j sum_i g_i x_id cos(phi_ij) - z1_j sum_i g_i x_id sin(phi_ij)
+// (dL/dx is the pointwise kind kGradPos in gst_pointwise.cu.)
+//
+// The sums run over points for every mode -- the transpose of the forward
+// reduction.  A CTA keeps 512 modes in registers (2 per thread) and streams a
+// slice of the points through shared memory in chunks of 256; sin/cos are
+// recomputed from the phase instead of stored.  Point slices are spread over
+// blockIdx.y and the FP64 partial sums are added in slice order by a second
+// kernel, which also forms dL/dk.  FP64 (parity) and mixed precision (the
+// turn reduction of gst_mixed.cuh, SFU sin/cos, FP32 sums per chunk, FP64
+// across chunks) variants.
+#include <algorithm>
+
+#include "gst_common.cuh"
+#include "gst_mixed.cuh"
+
+namespace gst {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kModesPerThread = 2;
+constexpr int kModesPerCta = kThreads * kModesPerThread;
+constexpr int kChunk = 256;
+
+enum Prec { kF64 = 0, kMixed = 1 };
+
+struct VjpArgs {
+    int64_t n_modes, n_pts;
+    const double *cov, *pos, *g;
+    int64_t pts_per_split;
+    double *partial;  // [split][n_modes][2 + 2 dim]
+};
+
+template <int DIM, int PREC>
+__global__ void __launch_bounds__(kThreads) vjp_modes_kernel(const VjpArgs a) {
+    constexpr int NA = 2 + 2 * DIM;  // C, S, Cx[d], Sx[d]
+    __shared__ double s_x[DIM][kChunk];
+    __shared__ double s_g[kChunk];
+    __shared__ float s_xh[DIM][kChunk], s_xl[DIM][kChunk], s_xf[DIM][kChunk];
+    __shared__ float s_gf[kChunk];
+
+    const int tid = threadIdx.x;
+    int64_t mode[kModesPerThread];
+    double k[kModesPerThread][DIM];
+    float qh[kModesPerThread][3], ql[kModesPerThread][3];
+#pragma unroll
+    for (int m = 0; m < kModesPerThread; ++m) {
+        mode[m] = static_cast<int64_t>(blockIdx.x) * kModesPerCta + m * kThreads + tid;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            k[m][d] = mode[m] < a.n_modes ? a.cov[d * a.n_modes + mode[m]] : 0.0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            constexpr double kInv2Pi = 0.15915494309189533576888376337251436;
+            const double q = d < DIM ? k[m][d] * kInv2Pi : 0.0;
+            qh[m][d] = split_hi12(q);
+            ql[m][d] = static_cast<float>(q - static_cast<double>(qh[m][d]));
+        }
+    }
+    double acc[kModesPerThread][NA];
+#pragma unroll
+    for (int m = 0; m < kModesPerThread; ++m)
+#pragma unroll
+        for (int c = 0; c < NA; ++c) acc[m][c] = 0.0;
+
+    const int64_t p_begin = static_cast<int64_t>(blockIdx.y) * a.pts_per_split;
+    const int64_t p_end = min(p_begin + a.pts_per_split, a.n_pts);
+    for (int64_t c0 = p_begin; c0 < p_end; c0 += kChunk) {
+        const int64_t i = c0 + tid;
+        const bool in = i < p_end;
+        double xv[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xv[d] = in ? a.pos[d * a.n_pts + i] : 0.0;
+        const double gv = in ? a.g[i] : 0.0;  // g = 0 pads the chunk
+        if (PREC == kF64) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) s_x[d][tid] = xv[d];
+            s_g[tid] = gv;
+        } else {
+            const MixedPoint<DIM> mp = mixed_split_point<DIM>(xv);
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                s_xh[d][tid] = mp.xh[d];
+                s_xl[d][tid] = mp.xl[d];
+                s_xf[d][tid] = mp.xf[d];
+            }
+            s_gf[tid] = static_cast<float>(gv);
+        }
+        __syncthreads();
+        const int n = static_cast<int>(min(static_cast<int64_t>(kChunk), p_end - c0));
+        if (PREC == kF64) {
+            for (int p = 0; p < n; ++p) {
+                const double gp = s_g[p];
+                double xp[DIM];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) xp[d] = s_x[d][p];
+#pragma unroll
+                for (int m = 0; m < kModesPerThread; ++m) {
+                    double ph = k[m][0] * xp[0];
+#pragma unroll
+                    for (int d = 1; d < DIM; ++d) ph = fma(k[m][d], xp[d], ph);
+                    double sn, cs;
+                    sincos(ph, &sn, &cs);
+                    const double gc = gp * cs, gs = gp * sn;
+                    acc[m][0] += gc;
+                    acc[m][1] += gs;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) {
+                        acc[m][2 + d] = fma(gc, xp[d], acc[m][2 + d]);
+                        acc[m][2 + DIM + d] = fma(gs, xp[d], acc[m][2 + DIM + d]);
+                    }
+                }
+            }
+        } else {
+            float af[kModesPerThread][NA];
+#pragma unroll
+            for (int m = 0; m < kModesPerThread; ++m)
+#pragma unroll
+                for (int c = 0; c < NA; ++c) af[m][c] = 0.0f;
+            for (int p = 0; p < n; ++p) {
+                MixedPoint<DIM> mp;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    mp.xh[d] = s_xh[d][p];
+                    mp.xl[d] = s_xl[d][p];
+                    mp.xf[d] = s_xf[d][p];
+                }
+                const float gp = s_gf[p];
+#pragma unroll
+                for (int m = 0; m < kModesPerThread; ++m) {
+                    float sn, cs;
+                    mixed_sincos<DIM>(qh[m], ql[m], mp, &sn, &cs);
+                    const float gc = gp * cs, gs = gp * sn;
+                    af[m][0] += gc;
+                    af[m][1] += gs;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) {
+                        af[m][2 + d] = fmaf(gc, mp.xf[d], af[m][2 + d]);
+                        af[m][2 + DIM + d] = fmaf(gs, mp.xf[d], af[m][2 + DIM + d]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < kModesPerThread; ++m)
+#pragma unroll
+                for (int c = 0; c < NA; ++c) acc[m][c] += static_cast<double>(af[m][c]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int m = 0; m < kModesPerThread; ++m) {
+        if (mode[m] >= a.n_modes) continue;
+        double *dst = a.partial + (static_cast<int64_t>(blockIdx.y) * a.n_modes + mode[m]) * NA;
+#pragma unroll
+        for (int c = 0; c < NA; ++c) dst[c] = acc[m][c];
+    }
+}
+
+// Sums the slices in order and forms the gradients.
+__global__ void vjp_modes_finish_kernel(int dim, int64_t n_modes, int64_t n_split,
+                                        const double *__restrict__ partial,
+                                        const double *__restrict__ z1,
+                                        const double *__restrict__ z2,
+                                        double *grad_z1, double *grad_z2,
+                                        double *grad_cov) {
+    const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (j >= n_modes) return;
+    const int na = 2 + 2 * dim;
+    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t k = 0; k < n_split; ++k) {
+        const double *src = partial + (k * n_modes + j) * na;
+        for (int c = 0; c < na; ++c) s[c] += src[c];
+    }
+    if (grad_z1) grad_z1[j] = s[0];
+    if (grad_z2) grad_z2[j] = s[1];
+    if (grad_cov)
+        for (int d = 0; d < dim; ++d)
+            grad_cov[d * n_modes + j] = z2[j] * s[2 + d] - z1[j] * s[2 + dim + d];
+}
+
+template <int PREC>
+cudaError_t launch_vjp(int dim, dim3 grid, const VjpArgs &args, cudaStream_t s) {
+    switch (dim) {
+        case 1: vjp_modes_kernel<1, PREC><<<grid, kThreads, 0, s>>>(args); break;
+        case 2: vjp_modes_kernel<2, PREC><<<grid, kThreads, 0, s>>>(args); break;
+        case 3: vjp_modes_kernel<3, PREC><<<grid, kThreads, 0, s>>>(args); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+int run_vjp_modes(int prec, int dim, int64_t n_modes, int64_t n_pts,
+                  const double *cov, const double *z1, const double *z2,
+                  const double *pos, const double *g, double *grad_z1,
+                  double *grad_z2, double *grad_cov, cudaStream_t s) {
+    if (dim < 1 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
+    if (n_modes < 0 || n_pts < 0) return GST_ERR_INVALID_ARGUMENT;
+    if (n_modes == 0) return GST_OK;
+    if (cov == nullptr || z1 == nullptr || z2 == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    if (current_device() < 0) return GST_ERR_NO_DEVICE;
+    if (n_pts == 0) {
+        if (grad_z1) GST_TRY_CUDA(cudaMemsetAsync(grad_z1, 0, 8 * n_modes, s));
+        if (grad_z2) GST_TRY_CUDA(cudaMemsetAsync(grad_z2, 0, 8 * n_modes, s));
+        if (grad_cov) GST_TRY_CUDA(cudaMemsetAsync(grad_cov, 0, 8 * n_modes * dim, s));
+        return GST_OK;
+    }
+    if (pos == nullptr || g == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    const int64_t mode_blocks = ceil_div(n_modes, kModesPerCta);
+    if (mode_blocks > 0x7fffffffLL) return GST_ERR_TOO_LARGE;
+    // slices of points: about four CTAs per SM, each slice >= one chunk
+    const int64_t target = static_cast<int64_t>(sm_count()) * 4;
+    int64_t n_split = std::max<int64_t>(1, ceil_div(target, mode_blocks));
+    n_split = std::min<int64_t>(n_split, ceil_div(n_pts, kChunk));
+    n_split = std::min<int64_t>(n_split, 65535);
+    const int64_t per = ceil_div(ceil_div(n_pts, n_split), kChunk) * kChunk;
+    n_split = ceil_div(n_pts, per);
+    const int na = 2 + 2 * dim;
+
+    StreamScratch ws;
+    GST_TRY_CUDA(ws.alloc(sizeof(double) * n_split * n_modes * na, s));
+    VjpArgs args{n_modes, n_pts, cov, pos, g, per, static_cast<double *>(ws.ptr)};
+    const dim3 grid(static_cast<unsigned>(mode_blocks), static_cast<unsigned>(n_split));
+    GST_TRY_CUDA(prec == kF64 ? launch_vjp<kF64>(dim, grid, args, s)
+                              : launch_vjp<kMixed>(dim, grid, args, s));
+    vjp_modes_finish_kernel<<<static_cast<unsigned>(ceil_div(n_modes, 256)), 256, 0, s>>>(
+        dim, n_modes, n_split, args.partial, z1, z2, grad_z1, grad_z2, grad_cov);
+    GST_TRY_CUDA(cudaGetLastError());
+    return GST_OK;
+}
+
+}  // namespace
+}  // namespace gst
+
+extern "C" {
+
+int gst_summate_vjp_modes_f64(int dim, int64_t n_modes, int64_t n_pts,
+                              const double *cov_samples, const double *z_1,
+                              const double *z_2, const double *pos,
+                              const double *grad_out, double *grad_z1,
+                              double *grad_z2, double *grad_cov, void *stream) {
+    return gst::run_vjp_modes(gst::kF64, dim, n_modes, n_pts, cov_samples, z_1,
+                              z_2, pos, grad_out, grad_z1, grad_z2, grad_cov,
+                              static_cast<cudaStream_t>(stream));
+}
+
+int gst_summate_vjp_modes_mixed(int dim, int64_t n_modes, int64_t n_pts,
+                                const double *cov_samples, const double *z_1,
+                                const double *z_2, const double *pos,
+                                const double *grad_out, double *grad_z1,
+                                double *grad_z2, double *grad_cov, void *stream) {
+    return gst::run_vjp_modes(gst::kMixed, dim, n_modes, n_pts, cov_samples, z_1,
+                              z_2, pos, grad_out, grad_z1, grad_z2, grad_cov,
+                              static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -26,6 +26,7 @@
 #include <mutex>
 
 #include "gst_common.cuh"
+#include "gst_mixed.cuh"
 
 namespace gst {
 namespace {
@@ -33,7 +34,11 @@ namespace {
 constexpr int kEntryBytes = 64;  // one packed mode
 constexpr int kStages = 2;
 
-enum Kind { kScalar = 0, kIncompr = 1 };
+// kGradPos: the position adjoint of summate,
+//   out[d, i] = sum_j k_jd (z2_j cos(<k_j, x_i>) - z1_j sin(<k_j, x_i>)),
+// evaluated like the incompressible sum with "projector" k and amplitudes
+// (z2, -z1).
+enum Kind { kScalar = 0, kIncompr = 1, kGradPos = 2 };
 enum Prec { kF64 = 0, kMixed = 1 };
 enum PosMode { kUnstructured = 0, kStructured = 1 };
 
@@ -54,9 +59,6 @@ struct Tiling<kMixed> {
     static constexpr int kMinBlocks = 2;
 };
 
-// Magic constant for round-to-nearest-integer by addition (|v| < 2^22).
-constexpr float kRoundMagic = 12582912.0f;  // 1.5 * 2^23
-constexpr double kPi = 3.141592653589793238462643383279502884;
 
 // ---------------------------------------------------------- mode packing --
 //
@@ -92,6 +94,11 @@ __global__ void pack_modes_kernel(int dim, int64_t n_modes, int64_t n_padded,
         w = weight ? weight[j] : 1.0;
         a1 = z1[j];
         a2 = z2[j];
+        if (KIND == kGradPos) {
+            a1 = z2[j];
+            a2 = -z1[j];
+            for (int d = 0; d < dim && d < 3; ++d) proj[d] = k[d];
+        }
         if (KIND == kIncompr) {
             // p_c = delta_c0 - k_c k_0 / |k|^2   (generator.py:479-495)
             double k2 = 0.0;
@@ -105,6 +112,7 @@ __global__ void pack_modes_kernel(int dim, int64_t n_modes, int64_t n_padded,
         double *e = static_cast<double *>(table) + j * 8;
         if (KIND == kScalar) {
             for (int d = 0; d < 4; ++d) e[d] = k[d];
+            // (kIncompr and kGradPos share the layout below)
             e[4] = a1;
             e[5] = a2;
             e[6] = w;
@@ -116,19 +124,8 @@ __global__ void pack_modes_kernel(int dim, int64_t n_modes, int64_t n_padded,
             for (int d = 0; d < 3; ++d) e[5 + d] = proj[d];
         }
     } else {
-        a1 *= w;
-        a2 *= w;
-        float *e = static_cast<float *>(table) + j * 16;
-        for (int d = 0; d < 3; ++d) {
-            const double q = k[d] / (2.0 * kPi);
-            const float qh = split_hi12(q);
-            e[d] = qh;
-            e[4 + d] = static_cast<float>(q - static_cast<double>(qh));
-            e[8 + d] = static_cast<float>(proj[d]);
-        }
-        e[3] = static_cast<float>(a1);
-        e[7] = static_cast<float>(a2);
-        for (int d = 11; d < 16; ++d) e[d] = 0.0f;
+        mixed_pack_entry(static_cast<float *>(table) + j * 16, k, a1 * w, a2 * w,
+                         proj);
     }
 }
 
@@ -176,7 +173,7 @@ __global__ void __launch_bounds__(Tiling<PREC>::kThreads,
     constexpr int P = T::kPoints;
     constexpr int NT = T::kThreads;
     constexpr int TILE = T::kTileModes;
-    constexpr int NC = (KIND == kIncompr) ? DIM : 1;  // output components
+    constexpr int NC = (KIND == kScalar) ? 1 : DIM;  // output components
     constexpr uint32_t kStageBytes = TILE * kEntryBytes;
 
     __shared__ __align__(128) unsigned char stage[kStages][kStageBytes];
@@ -204,17 +201,10 @@ __global__ void __launch_bounds__(Tiling<PREC>::kThreads,
     }
 
     // Mixed precision: positions split once per point.
-    float xh[P][DIM], xl[P][DIM], xf[P][DIM];
+    MixedPoint<DIM> mp[P];
     if (PREC == kMixed) {
 #pragma unroll
-        for (int p = 0; p < P; ++p)
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                xh[p][d] = split_hi12(x[p][d]);
-                xl[p][d] = static_cast<float>(x[p][d] -
-                                              static_cast<double>(xh[p][d]));
-                xf[p][d] = static_cast<float>(x[p][d]);
-            }
+        for (int p = 0; p < P; ++p) mp[p] = mixed_split_point<DIM>(x[p]);
     }
 
     double acc[P][NC];
@@ -282,28 +272,12 @@ __global__ void __launch_bounds__(Tiling<PREC>::kThreads,
                 const float qh[3] = {qa.x, qa.y, qa.z};
                 const float ql[3] = {qb.x, qb.y, qb.z};
                 float4 pr = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (KIND == kIncompr) pr = e[2];
+                if (KIND != kScalar) pr = e[2];
                 const float prj[3] = {pr.x, pr.y, pr.z};
 #pragma unroll
                 for (int p = 0; p < P; ++p) {
-                    // turns t = q . x, reduced exactly: qh*xh is exact, its
-                    // integer part drops out; the cross terms carry the rest.
-                    float r = 0.0f, cross = 0.0f;
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d) {
-                        const float prod = __fmul_rn(qh[d], xh[p][d]);
-                        const float nint =
-                            __fsub_rn(__fadd_rn(prod, kRoundMagic), kRoundMagic);
-                        const float frac = __fsub_rn(prod, nint);
-                        r = (d == 0) ? frac : __fadd_rn(r, frac);
-                        cross = fmaf(qh[d], xl[p][d], cross);
-                        cross = fmaf(ql[d], xf[p][d], cross);
-                    }
-                    r = __fadd_rn(r, cross);
-                    r = __fsub_rn(r, __fsub_rn(__fadd_rn(r, kRoundMagic),
-                                               kRoundMagic));
                     float sn, cs;
-                    __sincosf(r * 6.28318530717958647692f, &sn, &cs);
+                    mixed_sincos<DIM>(qh, ql, mp[p], &sn, &cs);
                     if (KIND == kScalar) {
                         accf[p][0] = fmaf(qa.w, cs, fmaf(qb.w, sn, accf[p][0]));
                     } else {
@@ -397,6 +371,14 @@ cudaError_t launch_main(dim3 grid, const PointwiseArgs &args, cudaStream_t s) {
 template <int KIND, int PREC, int POS>
 cudaError_t dispatch_dim(int dim, dim3 grid, const PointwiseArgs &args,
                          cudaStream_t s) {
+    if (KIND == kGradPos) {
+        switch (dim) {
+            case 1: return launch_main<1, KIND, PREC, POS>(grid, args, s);
+            case 2: return launch_main<2, KIND, PREC, POS>(grid, args, s);
+            case 3: return launch_main<3, KIND, PREC, POS>(grid, args, s);
+            default: return cudaErrorInvalidValue;
+        }
+    }
     if (KIND == kIncompr) {
         switch (dim) {
             case 2: return launch_main<2, KIND, PREC, POS>(grid, args, s);
@@ -434,9 +416,11 @@ void pack(const Request &r, int64_t n_padded, void *table) {
 }
 
 int run(const Request &r) {
-    const int nc = (r.kind == kIncompr) ? r.dim : 1;
+    const int nc = (r.kind == kScalar) ? 1 : r.dim;
     if (r.kind == kIncompr) {
         if (r.dim < 2 || r.dim > 3) return GST_ERR_UNSUPPORTED_DIM;
+    } else if (r.kind == kGradPos) {
+        if (r.dim < 1 || r.dim > 3) return GST_ERR_UNSUPPORTED_DIM;
     } else {
         const int max_dim = (r.prec == kF64) ? 4 : 3;
         if (r.dim < 1 || r.dim > max_dim) return GST_ERR_UNSUPPORTED_DIM;
@@ -504,9 +488,12 @@ int run(const Request &r) {
     if (r.kind == kScalar) {
         if (r.prec == kF64) pack<kScalar, kF64>(r, n_padded, table);
         else pack<kScalar, kMixed>(r, n_padded, table);
-    } else {
+    } else if (r.kind == kIncompr) {
         if (r.prec == kF64) pack<kIncompr, kF64>(r, n_padded, table);
         else pack<kIncompr, kMixed>(r, n_padded, table);
+    } else {
+        if (r.prec == kF64) pack<kGradPos, kF64>(r, n_padded, table);
+        else pack<kGradPos, kMixed>(r, n_padded, table);
     }
     GST_TRY_CUDA(cudaGetLastError());
 
@@ -535,9 +522,12 @@ int run(const Request &r) {
     if (r.kind == kScalar)
         e = (r.prec == kF64) ? dispatch<kScalar, kF64>(r.pos_mode, r.dim, grid, args, r.stream)
                              : dispatch<kScalar, kMixed>(r.pos_mode, r.dim, grid, args, r.stream);
-    else
+    else if (r.kind == kIncompr)
         e = (r.prec == kF64) ? dispatch<kIncompr, kF64>(r.pos_mode, r.dim, grid, args, r.stream)
                              : dispatch<kIncompr, kMixed>(r.pos_mode, r.dim, grid, args, r.stream);
+    else
+        e = (r.prec == kF64) ? dispatch<kGradPos, kF64>(r.pos_mode, r.dim, grid, args, r.stream)
+                             : dispatch<kGradPos, kMixed>(r.pos_mode, r.dim, grid, args, r.stream);
     GST_TRY_CUDA(e);
 
     if (n_split > 1) {
@@ -623,6 +613,26 @@ int gst_summate_fourier_f64(int dim, int64_t n_modes, int64_t n_pts,
     auto r = gst::make_request(gst::kScalar, gst::kF64, dim, n_modes, n_pts,
                                modes, z_1, z_2, pos, out, GST_OUT_F64, stream);
     r.weight = spectrum_factor;
+    return gst::run(r);
+}
+
+int gst_summate_vjp_pos_f64(int dim, int64_t n_modes, int64_t n_pts,
+                            const double *cov_samples, const double *z_1,
+                            const double *z_2, const double *pos, double *out,
+                            void *stream) {
+    auto r = gst::make_request(gst::kGradPos, gst::kF64, dim, n_modes, n_pts,
+                               cov_samples, z_1, z_2, pos, out, GST_OUT_F64,
+                               stream);
+    return gst::run(r);
+}
+
+int gst_summate_vjp_pos_mixed(int dim, int64_t n_modes, int64_t n_pts,
+                              const double *cov_samples, const double *z_1,
+                              const double *z_2, const double *pos, double *out,
+                              void *stream) {
+    auto r = gst::make_request(gst::kGradPos, gst::kMixed, dim, n_modes, n_pts,
+                               cov_samples, z_1, z_2, pos, out, GST_OUT_F64,
+                               stream);
     return gst::run(r);
 }
 

@@ -213,6 +213,66 @@ int gst_grid_tc_contract(int dim, int64_t n_modes, const int64_t *axis_len,
                          void *out, int out_type, double scale, void *stream);
 
 /* ----------------------------------------------------------------------- */
+/* Adjoint of summate (no counterpart in the reference, which has no        */
+/* gradients).  For u = summate(cov_samples, z_1, z_2, pos) and an upstream */
+/* gradient grad_out = dL/du (n_pts,):                                      */
+/*   gst_summate_vjp_modes_*: grad_z1 (N,), grad_z2 (N,) and grad_cov       */
+/*     (dim, N) = dL/dz_1, dL/dz_2, dL/dk; any output may be NULL.          */
+/*   gst_summate_vjp_pos_*: v (dim, n_pts) with                             */
+/*     v[d, i] = sum_j k_jd (z2_j cos(<k_j, x_i>) - z1_j sin(<k_j, x_i>)),  */
+/*     so dL/dx[d, i] = grad_out[i] * v[d, i].                              */
+/* sin/cos are recomputed, nothing of the forward pass is stored.  dim 1..3.*/
+/* _f64 in FP64, _mixed with the mixed-precision phase reduction.           */
+/* ----------------------------------------------------------------------- */
+int gst_summate_vjp_modes_f64(int dim, int64_t n_modes, int64_t n_pts,
+                              const double *cov_samples, const double *z_1,
+                              const double *z_2, const double *pos,
+                              const double *grad_out, double *grad_z1,
+                              double *grad_z2, double *grad_cov, void *stream);
+int gst_summate_vjp_modes_mixed(int dim, int64_t n_modes, int64_t n_pts,
+                                const double *cov_samples, const double *z_1,
+                                const double *z_2, const double *pos,
+                                const double *grad_out, double *grad_z1,
+                                double *grad_z2, double *grad_cov, void *stream);
+int gst_summate_vjp_pos_f64(int dim, int64_t n_modes, int64_t n_pts,
+                            const double *cov_samples, const double *z_1,
+                            const double *z_2, const double *pos, double *out,
+                            void *stream);
+int gst_summate_vjp_pos_mixed(int dim, int64_t n_modes, int64_t n_pts,
+                              const double *cov_samples, const double *z_1,
+                              const double *z_2, const double *pos, double *out,
+                              void *stream);
+
+/* ----------------------------------------------------------------------- */
+/* Batched ensembles: many realizations with their own modes and point sets. */
+/* The reference generates an ensemble by looping over seeds, one summate   */
+/* call per realization (examples/01_random_field/01_srf_ensemble.py); here */
+/* the ensemble is one persistent launch over a queue of (realization,      */
+/* point tile) work items, longest first.  Realization r owns modes        */
+/* [sum(mode_counts[:r]), +mode_counts[r]) of cov (dim, total_modes), z_1,  */
+/* z_2 and points [sum(point_counts[:r]), +point_counts[r]) of pos          */
+/* (dim, total_points) and out (total_points,).  mode_counts and            */
+/* point_counts are HOST arrays; scales (device, n_items, may be NULL)      */
+/* multiplies each realization's result (sqrt(var_r / N_r) for RandMeth).   */
+/* Arithmetic: the mixed-precision path.  variant selects the tile shape    */
+/* (0: 512 points per tile, 1: 1024).  gst_batch_prepare (synchronous, once */
+/* per ensemble shape) writes the work list into the caller's workspace;   */
+/* gst_batch_run is asynchronous, allocates nothing and may be captured in  */
+/* a CUDA graph; it must see the same counts and variant as prepare.        */
+/* ----------------------------------------------------------------------- */
+int gst_batch_workspace_size(int dim, int64_t n_items, const int64_t *mode_counts,
+                             const int64_t *point_counts, int variant,
+                             size_t *bytes);
+int gst_batch_prepare(int dim, int64_t n_items, const int64_t *mode_counts,
+                      const int64_t *point_counts, int variant, void *workspace,
+                      size_t workspace_bytes, void *stream);
+int gst_batch_run(int dim, int64_t n_items, const int64_t *mode_counts,
+                  const int64_t *point_counts, int variant, const double *cov,
+                  const double *z_1, const double *z_2, const double *pos,
+                  const double *scales, void *out, int out_type,
+                  void *workspace, size_t workspace_bytes, void *stream);
+
+/* ----------------------------------------------------------------------- */
 /* Diagnostics (no reference counterpart).                                  */
 /* ----------------------------------------------------------------------- */
 

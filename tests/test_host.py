@@ -205,3 +205,16 @@ def test_summators_refuse_without_gpu():
         pytest.skip("a CUDA device is present")
     with pytest.raises(RuntimeError):
         gg.summate(np.ones((2, 3)), np.ones(3), np.ones(3), np.ones((2, 4)))
+
+
+def test_torch_isometrize_matches_numpy():
+    import torch
+
+    from gstools_gb300.grad import isometrize_matrix
+
+    for dim, angles, anis in ((2, [0.7], [0.4]), (3, [0.3, 0.2, 0.1], [0.8, 0.6]),
+                              (3, [-1.1, 0.5, 2.0], [1.3, 0.2])):
+        ref = matrix_isometrize(dim, angles, anis)
+        got = isometrize_matrix(dim, torch.tensor(angles, dtype=torch.float64),
+                                torch.tensor(anis, dtype=torch.float64))
+        np.testing.assert_allclose(got.numpy(), ref, rtol=0, atol=1e-15)
