@@ -65,6 +65,11 @@ def parse():
     p.add_argument("--path", default="auto",
                    choices=["auto", "mixed", "tensor", "f64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="grid",
+                   choices=["grid", "points", "ensemble", "incompr", "adjoint"],
+                   help="grid: the headline (3-D Exponential, 256^3, 2000 "
+                        "modes); the others are the remaining BASELINE "
+                        "configurations")
     return p.parse_args()
 
 
@@ -347,9 +352,11 @@ def run_ours(args):
     slab = max(1, n // 16)
     lens64 = (ctypes.c_int64 * 4)(slab, n, n, 1)
     out64 = torch.empty((slab, n, n), dtype=torch.float64, device=dev)
+    d_axes64 = torch.from_numpy(np.concatenate(
+        [axes[0][:slab], axes[1], axes[2]])).to(dev)
 
     def step_f64():
-        _native.call("gst_summate_grid_f64", 3, N_MODES, lens64, p(d_axes),
+        _native.call("gst_summate_grid_f64", 3, N_MODES, lens64, p(d_axes64),
                      p(d_cov), p(d_z1), p(d_z2), p(out64), sp)
 
     t64, _ = timed([step_f64], 2, 1)
@@ -472,12 +479,308 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
 
 
+
+# ---------------------------------------------------------------------------
+# The other BASELINE configurations (not the headline; run explicitly with
+# --workload).  Each prints one JSON line with the same timing rules.
+# ---------------------------------------------------------------------------
+
+def _timed_events(torch, fn, steps, warmup, flush):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    return statistics.mean(times)
+
+
+def _line(args, workload, value, t_step, dtype, config, **extra):
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic", "config": dict(workload=workload, **config)}
+    line.update(extra)
+    return line
+
+
+def wl_points(args, torch, gg, flush):
+    """2-D Gaussian, var 1, len_scale 10, 1000 modes (reference RNG, seed
+    20170519), 100 000 points uniform in [0, 100]^2."""
+    import oracle
+
+    gen = gg.RandMeth(gg.Gaussian(dim=2, var=1.0, len_scale=10.0),
+                      mode_no=1000, seed=20170519)
+    pos = np.random.RandomState(20170519).uniform(0.0, 100.0, (2, 100_000))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+         for a in (gen.cov_samples, gen.z_1, gen.z_2, pos)]
+    work = 1000 * 100_000
+    f64 = lambda: gg.summate(*t)
+    mixed = lambda: gg.summate(*t, precision="mixed")
+    t64 = _timed_events(torch, f64, args.steps, args.warmup, flush)
+    tmx = _timed_events(torch, mixed, args.steps, args.warmup, flush)
+    ref = oracle.c_summate(gen.cov_samples, gen.z_1, gen.z_2, pos)
+    got64 = f64().cpu().numpy()
+    gotmx = mixed().cpu().numpy()
+    s = np.sqrt(1.0 / 1000)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        e2e = gg.summate(gen.cov_samples, gen.z_1, gen.z_2, pos, precision="mixed")
+    te2e = (time.perf_counter() - t0) / 3
+    return _line(
+        args, "gau2d_points100k_modes1000", work / tmx / 1e9, tmx,
+        "fp32 + exact turn reduction", {"points": 100_000, "modes": 1000},
+        f64_plain={"value": work / t64 / 1e9, "unit": UNIT,
+                   "max_rel_err_vs_oracle": float(np.max(np.abs(got64 - ref))
+                                                  / np.max(np.abs(ref)))},
+        error_vs_fp64={"rms_sigma": float(np.sqrt(np.mean((s * (gotmx - ref)) ** 2))),
+                       "max_abs_sigma": float(np.max(np.abs(s * (gotmx - ref))))},
+        e2e={"value": work / te2e / 1e9, "unit": UNIT,
+             "h2d_bytes_per_step": int(pos.nbytes + 4 * 8 * 1000),
+             "d2h_bytes_per_step": int(e2e.nbytes)},
+        gpu_launches=2 * args.steps)
+
+
+def make_ensemble(n_items=512, seed=20170519):
+    """512 realizations: 2-D Matern nu=1.5, var 1, len_scale log-uniform in
+    [2, 50], mode_no uniform in {1000, 2000, 4000}, own seed (MasterRNG) and
+    own point set of log-uniform size 1k-200k in [0, 500]^2."""
+    import gstools_gb300 as gg
+
+    seeds = gg.MasterRNG(seed)
+    rng = np.random.RandomState(seed + 1)
+    gens, pos = [], []
+    for _ in range(n_items):
+        ls = float(np.exp(rng.uniform(np.log(2.0), np.log(50.0))))
+        n_modes = int(rng.choice([1000, 2000, 4000]))
+        n_pts = int(np.exp(rng.uniform(np.log(1e3), np.log(2e5))))
+        gens.append(gg.RandMeth(gg.Matern(dim=2, nu=1.5, var=1.0, len_scale=ls),
+                                mode_no=n_modes, seed=seeds()))
+        pos.append(rng.uniform(0.0, 500.0, size=(2, n_pts)))
+    return gens, pos
+
+
+def wl_ensemble(args, torch, gg, flush):
+    from gstools_gb300 import _native
+
+    gens, pos = make_ensemble()
+    modes = [g.mode_no for g in gens]
+    pts = [p.shape[1] for p in pos]
+    work = int(sum(m * n for m, n in zip(modes, pts)))
+    scales = [np.sqrt(1.0 / m) for m in modes]
+    bs = gg.BatchedSummator(2, modes, pts, out_dtype="float32", graph=True)
+    bs.load([g.cov_samples for g in gens], [g.z_1 for g in gens],
+            [g.z_2 for g in gens], pos, scales)
+    tune = bs.tune()
+    t_batch = _timed_events(torch, bs.run, args.steps, args.warmup, flush)
+    batched = [f.astype(np.float64) for f in bs.split()]
+    # 512 sequential calls on the same device-resident data
+    cov, z1, z2, xx = bs.cov, bs.z1, bs.z2, bs.pos
+    outs = [torch.empty(n, dtype=torch.float64, device=bs.dev) for n in pts]
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    covs = [cov[:, bs.mode_off[r]:bs.mode_off[r + 1]].contiguous() for r in range(len(gens))]
+    poss = [xx[:, bs.point_off[r]:bs.point_off[r + 1]].contiguous() for r in range(len(gens))]
+
+    def sequential(name, extra):
+        for r in range(len(gens)):
+            m0, m1 = bs.mode_off[r], bs.mode_off[r + 1]
+            args_ = [2, modes[r], pts[r], ctypes.c_void_p(covs[r].data_ptr()),
+                     ctypes.c_void_p(z1[m0:m1].data_ptr()),
+                     ctypes.c_void_p(z2[m0:m1].data_ptr()),
+                     ctypes.c_void_p(poss[r].data_ptr()),
+                     ctypes.c_void_p(outs[r].data_ptr())] + extra + [stream]
+            _native.call(name, *args_)
+
+    t_seq64 = _timed_events(torch, lambda: sequential("gst_summate_f64", []),
+                            1, 1, flush)
+    ref = [o.cpu().numpy() * s for o, s in zip(outs, scales)]
+    t_seqmx = _timed_events(
+        torch, lambda: sequential("gst_summate_mixed", [_native.GST_OUT_F64]),
+        2, 1, flush)
+    err = np.sqrt(sum(float(np.sum((b - r) ** 2)) for b, r in zip(batched, ref))
+                  / sum(len(r) for r in ref))
+    mx = max(float(np.max(np.abs(b - r))) for b, r in zip(batched, ref))
+    # end to end: host arrays in, per-realization host arrays out
+    cov_l = [g.cov_samples for g in gens]
+    z1_l = [g.z_1 for g in gens]
+    z2_l = [g.z_2 for g in gens]
+    bs(cov_l, z1_l, z2_l, pos, scales)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = bs(cov_l, z1_l, z2_l, pos, scales)
+    te2e = time.perf_counter() - t0
+    return _line(
+        args, "matern2d_ensemble512", work / t_batch / 1e9, t_batch,
+        "fp32 + exact turn reduction",
+        {"realizations": len(gens), "mode_points_per_step": work,
+         "total_points": int(sum(pts)), "total_modes": int(sum(modes)),
+         "tile_variant": bs.variant, "autotune_ms": tune},
+        sequential_f64={"value": work / t_seq64 / 1e9, "unit": UNIT,
+                        "ms": t_seq64 * 1e3, "calls": len(gens)},
+        sequential_mixed={"value": work / t_seqmx / 1e9, "unit": UNIT,
+                          "ms": t_seqmx * 1e3, "calls": len(gens)},
+        value_over_sequential_f64=t_seq64 / t_batch,
+        error_vs_fp64={"rms_sigma": err, "max_abs_sigma": mx},
+        e2e={"value": work / te2e / 1e9, "unit": UNIT,
+             "h2d_bytes_per_step": int(sum(p.nbytes for p in pos)
+                                       + sum(c.nbytes for c in cov_l) * 2),
+             "d2h_bytes_per_step": int(sum(r.nbytes for r in res))},
+        gpu_launches=2 * args.steps)
+
+
+def wl_incompr(args, torch, gg, flush):
+    """3-D Gaussian incompressible field, var 1, len_scale 8, 2000 modes,
+    mean velocity 1, 192^3 unit grid, float32 3-component output."""
+    from gstools_gb300 import _native
+
+    data = np.load(os.path.join(ROOT, "tests", "golden", "workloads.npz"))
+    cov, z1, z2 = data["incompr3d/cov"], data["incompr3d/z1"], data["incompr3d/z2"]
+    n, nm = 192, 2000
+    scale = float(np.sqrt(1.0 / nm))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (cov, z1, z2)]
+    axes = torch.from_numpy(np.concatenate([np.arange(float(n))] * 3)).to(dev)
+    lens = (ctypes.c_int64 * 4)(n, n, n, 1)
+    out = torch.empty((3, n, n, n), dtype=torch.float32, device=dev)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    mixed = lambda: _native.call("gst_summate_incompr_grid_mixed", 3, nm, lens,
+                                 p(axes), p(d[0]), p(d[1]), p(d[2]), p(out),
+                                 _native.GST_OUT_F32, scale, stream)
+    tmx = _timed_events(torch, mixed, args.steps, args.warmup, flush)
+    slab = 12
+    lens64 = (ctypes.c_int64 * 4)(slab, n, n, 1)
+    out64 = torch.empty((3, slab, n, n), dtype=torch.float64, device=dev)
+    axes64 = torch.from_numpy(np.concatenate(
+        [np.arange(float(slab)), np.arange(float(n)), np.arange(float(n))])).to(dev)
+    f64 = lambda: _native.call("gst_summate_incompr_grid_f64", 3, nm, lens64,
+                               p(axes64), p(d[0]), p(d[1]), p(d[2]), p(out64),
+                               stream)
+    t64 = _timed_events(torch, f64, 1, 1, flush)
+    mixed()
+    got = out[:, :slab].double().cpu().numpy()
+    ref = scale * out64.cpu().numpy()
+    diff = got - ref
+    # divergence of the float32 field by central differences (unit spacing)
+    u = out.double()
+    div = ((u[0, 2:, 1:-1, 1:-1] - u[0, :-2, 1:-1, 1:-1])
+           + (u[1, 1:-1, 2:, 1:-1] - u[1, 1:-1, :-2, 1:-1])
+           + (u[2, 1:-1, 1:-1, 2:] - u[2, 1:-1, 1:-1, :-2])) / 2.0
+    grad_scale = ((u[0, 2:, 1:-1, 1:-1] - u[0, :-2, 1:-1, 1:-1]) / 2.0).std()
+    work = nm * n ** 3
+    return _line(
+        args, "gau3d_incompr_grid192_modes2000", work / tmx / 1e9, tmx,
+        "fp32 + exact turn reduction",
+        {"grid": [n] * 3, "modes": nm, "components": 3, "output": "float32"},
+        f64_plain={"value": nm * slab * n * n / t64 / 1e9, "unit": UNIT,
+                   "sample": f"{slab}x{n}x{n} slab"},
+        error_vs_fp64={"rms_sigma": float(np.sqrt(np.mean(diff ** 2))),
+                       "max_abs_sigma": float(np.max(np.abs(diff)))},
+        divergence={"fd_rms_over_grad_rms": float(div.std() / grad_scale),
+                    "note": "central differences, h=1; O(h^2) truncation"},
+        gpu_launches=2 * args.steps)
+
+
+def wl_adjoint(args, torch, gg, flush):
+    """3-D Gaussian, 4000 modes (reference RNG, anisotropic and rotated),
+    128^3 grid + 50 000 points in [0, 128]^3; loss = mean squared misfit at
+    10 000 random observation points against a field from another seed;
+    gradients w.r.t. z_1, z_2, len_scale, anisotropy and rotation angles."""
+    from gstools_gb300.grad import randmeth_field
+
+    data = np.load(os.path.join(ROOT, "tests", "golden", "workloads.npz"))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cov_ref = torch.tensor(data["gau3d_grad/cov"], device=dev)
+    z1 = torch.tensor(data["gau3d_grad/z1"], device=dev, requires_grad=True)
+    z2 = torch.tensor(data["gau3d_grad/z2"], device=dev, requires_grad=True)
+    rng = np.random.RandomState(7)
+    g = np.arange(128.0)
+    grid = np.array(np.meshgrid(g, g, g, indexing="ij")).reshape(3, -1)
+    pts = np.concatenate([grid, rng.uniform(0.0, 128.0, (3, 50_000))], axis=1)
+    x = torch.tensor(pts, device=dev)
+    obs = torch.tensor(rng.choice(pts.shape[1], 10_000, replace=False), device=dev)
+    other = gg.RandMeth(gg.Gaussian(dim=3, var=1.0, len_scale=16.0), mode_no=4000,
+                        seed=4242, sampling="analytic")
+    target = torch.tensor(other(pts[:, obs.cpu().numpy()], add_nugget=False),
+                          device=dev)
+    params = {"var": torch.tensor(1.0, dtype=torch.float64, device=dev),
+              "len_scale": torch.tensor(16.0, dtype=torch.float64, device=dev,
+                                        requires_grad=True),
+              "anis": torch.tensor([0.8, 0.6], dtype=torch.float64, device=dev,
+                                   requires_grad=True),
+              "angles": torch.tensor([0.3, 0.2, 0.1], dtype=torch.float64,
+                                     device=dev, requires_grad=True)}
+
+    def fwd(prec):
+        return randmeth_field(cov_ref, 16.0, z1, z2, x, precision=prec, **params)
+
+    def loss_of(u):
+        return torch.mean((u[obs] - target) ** 2)
+
+    def step_fwd():
+        with torch.no_grad():
+            fwd("mixed")
+
+    def step_fwd_bwd(prec="mixed"):
+        for t in (z1, z2, params["len_scale"], params["anis"], params["angles"]):
+            t.grad = None
+        loss_of(fwd(prec)).backward()
+
+    t_f = _timed_events(torch, step_fwd, args.steps, args.warmup, flush)
+    t_fb = _timed_events(torch, step_fwd_bwd, args.steps, args.warmup, flush)
+    grads_mixed = [t.grad.clone() for t in (z1, z2, params["len_scale"],
+                                            params["anis"], params["angles"])]
+    step_fwd_bwd("f64")
+    grads_f64 = [t.grad.clone() for t in (z1, z2, params["len_scale"],
+                                          params["anis"], params["angles"])]
+    rel = {name: float(torch.max(torch.abs(a - b)) / torch.max(torch.abs(b)))
+           for name, a, b in zip(("z1", "z2", "len_scale", "anis", "angles"),
+                                 grads_mixed, grads_f64)}
+    work = 4000 * pts.shape[1]
+    return _line(
+        args, "gau3d_adjoint_grid128_pts50k_modes4000", work / t_f / 1e9, t_f,
+        "fp32 + exact turn reduction",
+        {"points": int(pts.shape[1]), "modes": 4000, "observations": 10_000},
+        fwd_ms=t_f * 1e3, fwd_bwd_ms=t_fb * 1e3, fwd_bwd_over_fwd=t_fb / t_f,
+        grad_rel_err_mixed_vs_f64=rel, gpu_launches=None)
+
+
+def run_workload(args):
+    import torch
+
+    import gstools_gb300 as gg
+    from gstools_gb300 import build
+
+    torch.cuda.set_device(0)
+    build.build()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    fn = {"points": wl_points, "ensemble": wl_ensemble,
+          "incompr": wl_incompr, "adjoint": wl_adjoint}[args.workload]
+    clocks = Clocks(0)
+    clocks.start()
+    line = fn(args, torch, gg, flush)
+    line["clocks"] = clocks.stop()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.workload == "grid":
         run_ours(args)
+    else:
+        run_workload(args)
 
 
 if __name__ == "__main__":
