@@ -5,13 +5,14 @@
 // (src/gstools/field/generator.py:193-199 on the meshgrid of
 // src/gstools/tools/geometric.py:340-356) becomes
 //
-//     F[ix, iy, iz] = Re sum_j (w_j Ex[ix, j]) (Ey[iy, j] Ez[iz, j])
-//                   = sum_K A[ix, K] B[(iy, iz), K]
+//     F[(ix, iy), iz] = Re sum_j P_j(ix, iy) Q_j(iz),
+//     P_j = w_j Ex[ix, j] Ey[iy, j],   Q_j = Ez[iz, j]
 //
-// a real GEMM with K = 2N (real and imaginary parts), A = [Re(w Ex),
-// -Im(w Ex)] over the x axis and B = [Re(Ey Ez), Im(Ey Ez)] the Khatri-Rao
-// product over the (y, z) pairs.  A linear isometrize map M is folded into
-// the wave vectors by the caller (<k, M x> = <M^T k, x>).
+// a real GEMM with K = 2N (real and imaginary parts): rows are (x, y) pairs
+// (operand A = [Re P, -Im P], generated on the fly), columns are z points
+// (operand B = [Re Q, Im Q], a precomputed table).  A linear isometrize map
+// M is folded into the wave vectors by the caller (<k, M x> = <M^T k, x>).
+// A 2-D grid is the same with a dummy y axis of length 1 (Ey = 1).
 //
 // Precision: the per-axis tables come from an exact FP64 turn reduction of
 // k x / (2 pi) and an FP32 sincospi of the reduced angle; every operand is
@@ -23,17 +24,20 @@
 // registers of the epilogue threads.  Two accumulators alternate, so the
 // tensor cores fill one while the other is drained.
 //
-// Kernel structure (one CTA per output tile of 128 x-rows by 256 (y, z)
+// Kernel structure (one CTA per output tile of 128 (x, y) rows by 256 z
 // points, 320 threads):
-//   warp 0      bulk-copy (TMA) producer: per stage the pre-split A image
-//               (16 KB, already in the UMMA canonical K-major layout) and the
-//               stage's Ey / Ez table slices, into a 6-deep ring;
+//   warp 0      bulk-copy (TMA) producer: per 8-mode stage the pre-split
+//               TF32 image of Ez for the tile's 256 z points (32 KB, already
+//               in the UMMA canonical K-major layout) and the stage's w*Ex and
+//               Ey table slices, into a 4-deep ring;
 //   warp 1      allocates 512 TMEM columns (two 128 x 256 FP32 accumulators)
 //               and issues tcgen05.mma from one thread, M=128 N=256 K=8,
 //               3 MMAs per K-step;
-//   warps 2-9   generate B = Ey * Ez (complex product, TF32 split) into a
-//               3-deep ring of B slots, drain finished chunk accumulators
-//               into registers (tcgen05.ld), and store the scaled tile.
+//   warps 2-9   generate A = w Ex Ey (complex product, TF32 split; two
+//               threads per row) into a 4-deep ring of shared-memory slots,
+//               drain finished chunk accumulators into registers
+//               (tcgen05.ld), and store each row's 128-point z run with
+//               vector stores.
 // Every mbarrier wait is bounded (gst::mbar_wait); a timeout is recorded in
 // the device error word and the CTA still frees its tensor memory.
 #include <algorithm>
@@ -45,12 +49,12 @@ namespace {
 
 constexpr int kThreads = 320;
 constexpr int kGenThreads = 256;      // warps 2-9
-constexpr int kTileCols = 256;        // (y, z) points per tile (MMA N)
-constexpr int kXBlock = 128;          // x rows per tile (MMA M)
+constexpr int kTileRows = 128;        // (x, y) rows per tile (MMA M)
+constexpr int kTileCols = 256;        // z points per tile (MMA N)
 constexpr int kModesPerKStep = 4;     // 8 reals = K of one tf32 MMA
 constexpr int kKSteps = 2;            // K-steps per pipeline stage
 constexpr int kModesPerStage = kModesPerKStep * kKSteps;
-constexpr int kABlockBytes = 128 * 8 * 4;           // 128 rows x 8 tf32
+constexpr int kABlockBytes = kTileRows * 8 * 4;     // 128 rows x 8 tf32
 constexpr int kBBlockBytes = kTileCols * 8 * 4;     // 256 rows x 8 tf32
 constexpr int kAStageBytes = kKSteps * 2 * kABlockBytes;      // 16 KB
 constexpr int kBStageBytes = kKSteps * 2 * kBBlockBytes;      // 32 KB
@@ -172,24 +176,24 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 // ------------------------------------------------------------------ tables --
 
 struct GridGeom {
-    int64_t n[3];        // axis lengths (n[2] = 1 for 2-D)
+    int64_t n[3];        // x, y, z lengths (2-D: y is a dummy axis of length 1)
     int64_t off[3];      // offsets of the axes in the concatenated array
-    int64_t blocks[3];   // tiles along x (256), y (TY), z (TZ)
-    int tile[3];         // 256, TY, TZ
+    int src[3];          // caller axis feeding x, y, z (-1: dummy)
+    int64_t blocks[3];   // tiles along x (TX), y (TY), z (256)
+    int tile[3];         // TX, TY, 256 with TX * TY = 128
     int64_t n_stages;    // padded modes / kModesPerStage
     int64_t n_modes;
 };
 
-// One thread per (axis row, mode).  Axis 0 writes the pre-split A image,
-// axes 1 and 2 the complex tables Ey, Ez in per-stage blocks.
-__global__ void grid_tables_kernel(GridGeom g, int dim,
-                                   const double *__restrict__ cov,
+// One thread per (axis point, mode).  Axis x writes w*Ex, axis y writes Ey
+// (complex FP32, blocked [block][stage][mode][tile]); axis z writes the
+// pre-split TF32 image of [Re Ez, Im Ez] per 256-point block and stage.
+__global__ void grid_tables_kernel(GridGeom g, const double *__restrict__ cov,
                                    const double *__restrict__ z1,
                                    const double *__restrict__ z2,
                                    const double *__restrict__ axes,
-                                   unsigned char *__restrict__ a_image,
-                                   float2 *__restrict__ ey,
-                                   float2 *__restrict__ ez) {
+                                   float2 *__restrict__ wx, float2 *__restrict__ ey,
+                                   unsigned char *__restrict__ ez_image) {
     const int axis = blockIdx.z;
     const int64_t n_pad_modes = g.n_stages * kModesPerStage;
     const int64_t rows = g.blocks[axis] * g.tile[axis];
@@ -199,12 +203,12 @@ __global__ void grid_tables_kernel(GridGeom g, int dim,
     const int64_t r = idx / n_pad_modes;
 
     float c = 0.0f, s = 0.0f;
-    const bool live = (j < g.n_modes) && (r < g.n[axis]) &&
-                      (axis < dim || axis == 2);
+    const bool live = (j < g.n_modes) && (r < g.n[axis]);
     if (live) {
+        const int src = g.src[axis];
         double k = 0.0, x = 0.0;
-        if (axis < dim) {
-            k = cov[axis * g.n_modes + j];
+        if (src >= 0) {
+            k = cov[src * g.n_modes + j];
             x = axes[g.off[axis] + r];
         }
         // exact reduction of the phase to turns, FP32 sin/cos of the rest
@@ -214,37 +218,35 @@ __global__ void grid_tables_kernel(GridGeom g, int dim,
     }
     const int64_t st = j / kModesPerStage;
     const int mm = static_cast<int>(j % kModesPerStage);
+    const int tile = g.tile[axis];
+    const int64_t blk = r / tile;
+    const int t = static_cast<int>(r % tile);
     if (axis == 0) {
-        // a = w E with w = z1 - i z2: Re a = z1 c + z2 s, -Im a = z2 c - z1 s
-        float re = 0.0f, nim = 0.0f;
+        // w E with w = z1 - i z2
+        float re = 0.0f, im = 0.0f;
         if (live) {
             const double zz1 = z1[j], zz2 = z2[j];
             re = static_cast<float>(zz1 * c + zz2 * s);
-            nim = static_cast<float>(zz2 * c - zz1 * s);
+            im = static_cast<float>(zz1 * s - zz2 * c);
         }
-        const int64_t xb = r / kXBlock;
-        const uint32_t row = static_cast<uint32_t>(r % kXBlock);
+        wx[((blk * g.n_stages + st) * kModesPerStage + mm) * tile + t] =
+            make_float2(re, im);
+    } else if (axis == 1) {
+        ey[((blk * g.n_stages + st) * kModesPerStage + mm) * tile + t] =
+            make_float2(c, s);
+    } else {
         const int kstep = mm / kModesPerKStep;
         const uint32_t k0 = 2u * (mm % kModesPerKStep);
-        unsigned char *stage = a_image + (xb * g.n_stages + st) * kAStageBytes;
-        const float vals[2] = {re, nim};
+        unsigned char *stage = ez_image + (blk * g.n_stages + st) * kBStageBytes;
+        const float vals[2] = {c, s};
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             const float hi = to_tf32(vals[q]);
             const float lo = to_tf32(vals[q] - hi);
-            const uint32_t o = core_offset(row, k0 + q);
-            *reinterpret_cast<float *>(stage + (kstep * 2 + 0) * kABlockBytes +
-                                       o) = hi;
-            *reinterpret_cast<float *>(stage + (kstep * 2 + 1) * kABlockBytes +
-                                       o) = lo;
+            const uint32_t o = core_offset(static_cast<uint32_t>(t), k0 + q);
+            *reinterpret_cast<float *>(stage + (kstep * 2 + 0) * kBBlockBytes + o) = hi;
+            *reinterpret_cast<float *>(stage + (kstep * 2 + 1) * kBBlockBytes + o) = lo;
         }
-    } else {
-        const int tile = g.tile[axis];
-        const int64_t blk = r / tile;
-        const int t = static_cast<int>(r % tile);
-        float2 *tab = (axis == 1) ? ey : ez;
-        tab[((blk * g.n_stages + st) * kModesPerStage + mm) * tile + t] =
-            make_float2(c, s);
     }
 }
 
@@ -256,57 +258,55 @@ __device__ __forceinline__ int64_t ceil_div_dev(int64_t a, int64_t b) {
 
 struct GridArgs {
     GridGeom g;
-    const unsigned char *a_image;
+    const float2 *wx;
     const float2 *ey;
-    const float2 *ez;
+    const unsigned char *ez_image;
     void *out;
     int out_f32;
     double scale;
     unsigned int *err;
 };
 
-// Shared memory: a ring of bulk-copied slots (A image + Ey / Ez slices) and a
-// ring of generated B slots.  The copy ring is deeper so the bulk copies are
-// issued several stages ahead of the tensor cores; the B ring only has to
-// cover the generation time.
+// Shared memory: a ring of bulk-copied slots (Ez image + w*Ex and Ey slices)
+// and a ring of generated A slots.
 template <int TY>
 struct StageLayout {
-    static constexpr int TZ = kTileCols / TY;
+    static constexpr int TX = kTileRows / TY;
+    static constexpr int kWxBytes = kModesPerStage * TX * 8;
     static constexpr int kEyBytes = kModesPerStage * TY * 8;
-    static constexpr int kEzBytes = kModesPerStage * TZ * 8;
-    static constexpr int kA = 0;
-    static constexpr int kEy = kA + kAStageBytes;
-    static constexpr int kEz = kEy + kEyBytes;
-    static constexpr int kCopyBytes = kAStageBytes + kEyBytes + kEzBytes;
-    static constexpr int kSlotA = (kCopyBytes + 1023) / 1024 * 1024;
-    static constexpr int kSlotB = kBStageBytes;
-    static constexpr int kPipeB = 3;
+    static constexpr int kB = 0;
+    static constexpr int kWx = kB + kBStageBytes;
+    static constexpr int kEy = kWx + kWxBytes;
+    static constexpr int kCopyBytes = kBStageBytes + kWxBytes + kEyBytes;
+    static constexpr int kSlotB = (kCopyBytes + 1023) / 1024 * 1024;
+    static constexpr int kSlotA = kAStageBytes;
     static constexpr int kBudget = 227 * 1024 - 2048;
-    static constexpr int kPipeA0 = (kBudget - kPipeB * kSlotB) / kSlotA;
-    static constexpr int kPipeA = kPipeA0 > 6 ? 6 : kPipeA0;
-    static constexpr int kRingB = kPipeA * kSlotA;
-    static constexpr int kBars = kRingB + kPipeB * kSlotB;
+    static constexpr int kPipeA = 4;
+    static constexpr int kPipeB0 = (kBudget - kPipeA * kSlotA) / kSlotB;
+    static constexpr int kPipeB = kPipeB0 > 4 ? 4 : kPipeB0;
+    static constexpr int kRingA = kPipeB * kSlotB;
+    static constexpr int kBars = kRingA + kPipeA * kSlotA;
     static constexpr int kSmem = kBars + 1024 /*align*/ + 256 /*bars*/;
-    static_assert(kPipeA >= 3, "copy ring too shallow");
+    static_assert(kPipeB >= 3, "copy ring too shallow");
 };
 
 template <int TY>
 __global__ void __launch_bounds__(kThreads, 1)
     grid_tc_kernel(const GridArgs a) {
     using L = StageLayout<TY>;
-    constexpr int TZ = L::TZ;
-    constexpr int PA = L::kPipeA;
-    constexpr int PB = L::kPipeB;
+    constexpr int TX = L::TX;
+    constexpr int PB = L::kPipeB;   // copy ring (B operand + tables)
+    constexpr int PA = L::kPipeA;   // generated ring (A operand)
 
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::kBars);
-    uint64_t *full = bars;                 // [PA] bulk copies landed
-    uint64_t *empty = bars + PA;           // [PA] MMAs done with copy slot
-    uint64_t *bready = bars + 2 * PA;      // [PB] B generated
-    uint64_t *bfree = bars + 2 * PA + PB;  // [PB] MMAs done with B slot
-    uint64_t *chunk_done = bars + 2 * PA + 2 * PB;  // [2] accumulator done
+    uint64_t *full = bars;                 // [PB] bulk copies landed
+    uint64_t *empty = bars + PB;           // [PB] MMAs done with copy slot
+    uint64_t *aready = bars + 2 * PB;      // [PA] A generated
+    uint64_t *afree = bars + 2 * PB + PA;  // [PA] MMAs done with A slot
+    uint64_t *chunk_done = bars + 2 * PB + 2 * PA;  // [2] accumulator done
     uint64_t *acc_free = chunk_done + 2;            // [2] accumulator drained
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_free + 2);
 
@@ -322,13 +322,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int64_t n_chunks = ceil_div_dev(n_st, kChunkStages);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < PA; ++s) {
+        for (int s = 0; s < PB; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        for (int s = 0; s < PB; ++s) {
-            mbar_init(&bready[s], kGenThreads / 32);
-            mbar_init(&bfree[s], 1);
+        for (int s = 0; s < PA; ++s) {
+            mbar_init(&aready[s], kGenThreads / 32);
+            mbar_init(&afree[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&chunk_done[b], 1);
@@ -346,32 +346,32 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 0) {
         // ---------------------------------------------- bulk producer --
         if (lane == 0) {
-            const unsigned char *a_src = a.a_image + xb * n_st * kAStageBytes;
+            const unsigned char *ez_src = a.ez_image + zb * n_st * kBStageBytes;
+            const float2 *wx_src = a.wx + xb * n_st * kModesPerStage * TX;
             const float2 *ey_src = a.ey + yb * n_st * kModesPerStage * TY;
-            const float2 *ez_src = a.ez + zb * n_st * kModesPerStage * TZ;
             for (int64_t st = 0; st < n_st && ok; ++st) {
-                const int s = static_cast<int>(st % PA);
-                const uint32_t ph = static_cast<uint32_t>((st / PA) & 1);
+                const int s = static_cast<int>(st % PB);
+                const uint32_t ph = static_cast<uint32_t>((st / PB) & 1);
                 ok = mbar_wait(&empty[s], ph ^ 1u, a.err);
                 if (!ok) break;
-                unsigned char *dst = smem + s * L::kSlotA;
+                unsigned char *dst = smem + s * L::kSlotB;
                 mbar_arrive_expect_tx(&full[s], L::kCopyBytes);
-                bulk_copy_g2s(dst + L::kA, a_src + st * kAStageBytes,
-                              kAStageBytes, &full[s]);
+                bulk_copy_g2s(dst + L::kB, ez_src + st * kBStageBytes,
+                              kBStageBytes, &full[s]);
+                bulk_copy_g2s(dst + L::kWx, wx_src + st * kModesPerStage * TX,
+                              L::kWxBytes, &full[s]);
                 bulk_copy_g2s(dst + L::kEy, ey_src + st * kModesPerStage * TY,
                               L::kEyBytes, &full[s]);
-                bulk_copy_g2s(dst + L::kEz, ez_src + st * kModesPerStage * TZ,
-                              L::kEzBytes, &full[s]);
             }
         }
     } else if (warp == 1) {
         // ---------------------------------------------- MMA issuer --
         if (lane == 0) {
             for (int64_t st = 0; st < n_st && ok; ++st) {
-                const int sa = static_cast<int>(st % PA);
-                const uint32_t pha = static_cast<uint32_t>((st / PA) & 1);
                 const int sb = static_cast<int>(st % PB);
                 const uint32_t phb = static_cast<uint32_t>((st / PB) & 1);
+                const int sa = static_cast<int>(st % PA);
+                const uint32_t pha = static_cast<uint32_t>((st / PA) & 1);
                 const int64_t c = st / kChunkStages;
                 const int buf = static_cast<int>(c & 1);
                 const bool first = (st % kChunkStages) == 0;
@@ -381,35 +381,36 @@ __global__ void __launch_bounds__(kThreads, 1)
                                    static_cast<uint32_t>(((c >> 1) - 1) & 1), a.err);
                     if (!ok) break;
                 }
-                ok = mbar_wait(&full[sa], pha, a.err) &&
-                     mbar_wait(&bready[sb], phb, a.err);
+                ok = mbar_wait(&full[sb], phb, a.err) &&
+                     mbar_wait(&aready[sa], pha, a.err);
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t abase = smem_addr(smem + sa * L::kSlotA + L::kA);
-                const uint32_t bbase = smem_addr(smem + L::kRingB + sb * L::kSlotB);
+                const uint32_t bbase = smem_addr(smem + sb * L::kSlotB + L::kB);
+                const uint32_t abase = smem_addr(smem + L::kRingA + sa * L::kSlotA);
                 const uint32_t d = tmem + buf * 256;
 #pragma unroll
                 for (int ks = 0; ks < kKSteps; ++ks) {
                     const uint64_t bh = smem_desc(bbase + (ks * 2 + 0) * kBBlockBytes);
                     const uint64_t bl = smem_desc(bbase + (ks * 2 + 1) * kBBlockBytes);
-                    const uint32_t ablk = abase + ks * 2 * kABlockBytes;
-                    const uint64_t ah = smem_desc(ablk);
-                    const uint64_t al = smem_desc(ablk + kABlockBytes);
+                    const uint64_t ah = smem_desc(abase + (ks * 2 + 0) * kABlockBytes);
+                    const uint64_t al = smem_desc(abase + (ks * 2 + 1) * kABlockBytes);
                     const uint32_t acc = (first && ks == 0) ? 0u : 1u;
                     mma_tf32(d, ah, bh, acc);
                     mma_tf32(d, ah, bl, 1u);
                     mma_tf32(d, al, bh, 1u);
                 }
-                mma_commit(&empty[sa]);
-                mma_commit(&bfree[sb]);
+                mma_commit(&empty[sb]);
+                mma_commit(&afree[sa]);
                 if ((st % kChunkStages) == kChunkStages - 1 || st == n_st - 1)
                     mma_commit(&chunk_done[buf]);
             }
         }
     } else {
-        // ------------------------------------- B generators + epilogue --
-        const int gt = threadIdx.x - 64;       // 0..255: row of the B tile
-        const int yl = gt / TZ, zl = gt % TZ;
+        // ------------------------------------- A generators + epilogue --
+        const int gt = threadIdx.x - 64;       // 0..255
+        const int row = gt & (kTileRows - 1);  // (x, y) row of the A tile
+        const int ks_gen = gt >> 7;            // K-step this thread fills
+        const int xl = row / TY, yl = row % TY;
         const int q = warp & 3;                // TMEM lane quarter
         const int half = (warp - 2) >> 2;      // accumulator columns half
         const uint32_t t_row = tmem + (static_cast<uint32_t>(q * 32) << 16) +
@@ -442,50 +443,47 @@ __global__ void __launch_bounds__(kThreads, 1)
         };
 
         for (int64_t st = 0; st < n_st && ok; ++st) {
-            const int sa = static_cast<int>(st % PA);
-            const uint32_t pha = static_cast<uint32_t>((st / PA) & 1);
             const int sb = static_cast<int>(st % PB);
             const uint32_t phb = static_cast<uint32_t>((st / PB) & 1);
-            ok = mbar_wait(&bfree[sb], phb ^ 1u, a.err) &&
-                 mbar_wait(&full[sa], pha, a.err);
+            const int sa = static_cast<int>(st % PA);
+            const uint32_t pha = static_cast<uint32_t>((st / PA) & 1);
+            ok = mbar_wait(&afree[sa], pha ^ 1u, a.err) &&
+                 mbar_wait(&full[sb], phb, a.err);
             if (__any_sync(0xffffffffu, !ok)) { ok = false; break; }
-            const unsigned char *slot = smem + sa * L::kSlotA;
+            const unsigned char *slot = smem + sb * L::kSlotB;
+            const float2 *swx = reinterpret_cast<const float2 *>(slot + L::kWx);
             const float2 *sey = reinterpret_cast<const float2 *>(slot + L::kEy);
-            const float2 *sez = reinterpret_cast<const float2 *>(slot + L::kEz);
-            unsigned char *bslot = smem + L::kRingB + sb * L::kSlotB;
+            float hi[8], lo[8];
 #pragma unroll
-            for (int ks = 0; ks < kKSteps; ++ks) {
-                float hi[8], lo[8];
+            for (int m = 0; m < kModesPerKStep; ++m) {
+                const int mm = ks_gen * kModesPerKStep + m;
+                const float2 p = swx[mm * TX + xl];
+                const float2 e = sey[mm * TY + yl];
+                const float re = fmaf(p.x, e.x, -p.y * e.y);
+                const float im = fmaf(p.x, e.y, p.y * e.x);
+                hi[2 * m] = to_tf32(re);
+                lo[2 * m] = re - hi[2 * m];   // the MMA reads lo as TF32
+                hi[2 * m + 1] = to_tf32(-im);
+                lo[2 * m + 1] = -im - hi[2 * m + 1];
+            }
+            unsigned char *aslot = smem + L::kRingA + sa * L::kSlotA;
+            unsigned char *ah = aslot + (ks_gen * 2 + 0) * kABlockBytes;
+            unsigned char *al = aslot + (ks_gen * 2 + 1) * kABlockBytes;
 #pragma unroll
-                for (int m = 0; m < kModesPerKStep; ++m) {
-                    const int mm = ks * kModesPerKStep + m;
-                    const float2 p = sey[mm * TY + yl];
-                    const float2 r = sez[mm * TZ + zl];
-                    const float re = fmaf(p.x, r.x, -p.y * r.y);
-                    const float im = fmaf(p.x, r.y, p.y * r.x);
-                    hi[2 * m] = to_tf32(re);
-                    lo[2 * m] = to_tf32(re - hi[2 * m]);
-                    hi[2 * m + 1] = to_tf32(im);
-                    lo[2 * m + 1] = to_tf32(im - hi[2 * m + 1]);
-                }
-                unsigned char *bh = bslot + (ks * 2 + 0) * kBBlockBytes;
-                unsigned char *bl = bslot + (ks * 2 + 1) * kBBlockBytes;
-#pragma unroll
-                for (int kb = 0; kb < 2; ++kb) {
-                    const uint32_t o = core_offset(gt, kb * 4);
-                    *reinterpret_cast<float4 *>(bh + o) = make_float4(
-                        hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
-                    *reinterpret_cast<float4 *>(bl + o) = make_float4(
-                        lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
-                }
+            for (int kb = 0; kb < 2; ++kb) {
+                const uint32_t o = core_offset(row, kb * 4);
+                *reinterpret_cast<float4 *>(ah + o) = make_float4(
+                    hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
+                *reinterpret_cast<float4 *>(al + o) = make_float4(
+                    lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
             }
             fence_async_smem();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&bready[sb]);
+            if (lane == 0) mbar_arrive(&aready[sa]);
             // Drain the previous chunk once the MMAs are past it: generating
-            // stage st needed the MMAs of stage st - PB to be complete.
+            // stage st needed the MMAs of stage st - PA to be complete.
             if (drained < n_chunks - 1 &&
-                st == (drained + 1) * kChunkStages - 1 + PB) {
+                st == (drained + 1) * kChunkStages - 1 + PA) {
                 ok = drain(drained);
                 ++drained;
             }
@@ -493,22 +491,35 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (; drained < n_chunks && ok; ++drained) ok = drain(drained);
 
         if (ok) {
-            const int64_t x = xb * kXBlock + q * 32 + lane;
-            const int64_t ny = g.n[1], nz = g.n[2];
-            if (x < g.n[0]) {
+            // this thread's accumulator row is TMEM lane q * 32 + lane
+            const int erow = q * 32 + lane;
+            const int64_t x = xb * TX + erow / TY;
+            const int64_t y = yb * TY + erow % TY;
+            const int64_t nz = g.n[2];
+            const int64_t z0 = zb * kTileCols + half * kColsPerThread;
+            if (x < g.n[0] && y < g.n[1] && z0 < nz) {
+                const int64_t base = (x * g.n[1] + y) * nz + z0;
+                const int64_t nvalid = min(static_cast<int64_t>(kColsPerThread), nz - z0);
+                const float sc = static_cast<float>(a.scale);
+                if (a.out_f32) {
+                    float *o = static_cast<float *>(a.out) + base;
+                    if (nvalid == kColsPerThread &&
+                        (reinterpret_cast<uintptr_t>(o) & 15u) == 0) {
 #pragma unroll
-                for (int i = 0; i < kColsPerThread; ++i) {
-                    const int n = half * kColsPerThread + i;
-                    const int64_t y = yb * TY + n / TZ;
-                    const int64_t z = zb * TZ + n % TZ;
-                    if (y < ny && z < nz) {
-                        const int64_t o = (x * ny + y) * nz + z;
-                        if (a.out_f32)
-                            static_cast<float *>(a.out)[o] =
-                                static_cast<float>(a.scale * acc[i]);
-                        else
-                            static_cast<double *>(a.out)[o] = a.scale * acc[i];
+                        for (int i = 0; i < kColsPerThread; i += 4)
+                            *reinterpret_cast<float4 *>(o + i) = make_float4(
+                                sc * acc[i], sc * acc[i + 1], sc * acc[i + 2],
+                                sc * acc[i + 3]);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < kColsPerThread; ++i)
+                            if (i < nvalid) o[i] = sc * acc[i];
                     }
+                } else {
+                    double *o = static_cast<double *>(a.out) + base;
+#pragma unroll
+                    for (int i = 0; i < kColsPerThread; ++i)
+                        if (i < nvalid) o[i] = a.scale * acc[i];
                 }
             }
         }
@@ -534,16 +545,10 @@ cudaError_t launch_grid(const GridArgs &args, int64_t n_tiles, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-}  // namespace
-}  // namespace gst
-
-namespace gst {
-namespace {
-
 struct GridPlan {
     GridGeom g;
-    int ty, tz;
-    size_t a_bytes, ey_off, ez_off, total;
+    int ty;
+    size_t wx_off, ey_off, ez_off, total;
 };
 
 int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
@@ -552,39 +557,48 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
     if (axis_len == nullptr || n_modes < 0) return GST_ERR_INVALID_ARGUMENT;
     GridGeom &g = p.g;
     g = GridGeom{};
-    int64_t total = 1, off = 0;
-    for (int d = 0; d < 3; ++d) {
-        g.n[d] = d < dim ? axis_len[d] : 1;
-        if (g.n[d] < 0) return GST_ERR_INVALID_ARGUMENT;
-        g.off[d] = off;
-        off += d < dim ? g.n[d] : 0;
-        total *= g.n[d];
+    int64_t total = 1;
+    for (int d = 0; d < dim; ++d) {
+        if (axis_len[d] < 0) return GST_ERR_INVALID_ARGUMENT;
+        total *= axis_len[d];
     }
     total_pts = total;
-    p.ty = dim == 3 ? 16 : kTileCols;
-    p.tz = kTileCols / p.ty;
-    g.tile[0] = kXBlock;
+    // caller axes -> (x, y, z); a 2-D grid uses a dummy y of length 1
+    if (dim == 3) {
+        g.src[0] = 0; g.src[1] = 1; g.src[2] = 2;
+        g.n[0] = axis_len[0]; g.n[1] = axis_len[1]; g.n[2] = axis_len[2];
+        g.off[0] = 0; g.off[1] = axis_len[0]; g.off[2] = axis_len[0] + axis_len[1];
+        p.ty = 16;
+    } else {
+        g.src[0] = 0; g.src[1] = -1; g.src[2] = 1;
+        g.n[0] = axis_len[0]; g.n[1] = 1; g.n[2] = axis_len[1];
+        g.off[0] = 0; g.off[1] = 0; g.off[2] = axis_len[0];
+        p.ty = 1;
+    }
+    g.tile[0] = kTileRows / p.ty;
     g.tile[1] = p.ty;
-    g.tile[2] = p.tz;
+    g.tile[2] = kTileCols;
     for (int d = 0; d < 3; ++d) g.blocks[d] = ceil_div(g.n[d], g.tile[d]);
     g.n_stages = ceil_div(n_modes, kModesPerStage);
     g.n_modes = n_modes;
     if (g.blocks[0] * g.blocks[1] * g.blocks[2] > 0x7fffffffLL)
         return GST_ERR_TOO_LARGE;
-    p.a_bytes = static_cast<size_t>(g.blocks[0]) * g.n_stages * kAStageBytes;
+    const size_t per_stage = kModesPerStage * sizeof(float2);
+    const size_t wx_bytes = static_cast<size_t>(g.blocks[0]) * g.n_stages *
+                            per_stage * g.tile[0];
     const size_t ey_bytes = static_cast<size_t>(g.blocks[1]) * g.n_stages *
-                            kModesPerStage * p.ty * sizeof(float2);
-    const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages *
-                            kModesPerStage * p.tz * sizeof(float2);
-    p.ey_off = align_up(p.a_bytes, 256);
-    p.ez_off = align_up(p.ey_off + ey_bytes, 256);
-    p.total = p.ez_off + ez_bytes;
+                            per_stage * g.tile[1];
+    const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages * kBStageBytes;
+    p.ez_off = 0;
+    p.wx_off = align_up(ez_bytes, 256);
+    p.ey_off = align_up(p.wx_off + wx_bytes, 256);
+    p.total = p.ey_off + ey_bytes;
     return GST_OK;
 }
 
-int run_tables(const GridPlan &p, int dim, const double *axes,
-               const double *cov, const double *z1, const double *z2,
-               unsigned char *ws, cudaStream_t s) {
+int run_tables(const GridPlan &p, const double *axes, const double *cov,
+               const double *z1, const double *z2, unsigned char *ws,
+               cudaStream_t s) {
     const GridGeom &g = p.g;
     const int64_t n_pad_modes = g.n_stages * kModesPerStage;
     int64_t max_rows = 0;
@@ -594,8 +608,8 @@ int run_tables(const GridPlan &p, int dim, const double *axes,
     const dim3 grid(static_cast<unsigned>(ceil_div(max_rows * n_pad_modes, threads)),
                     1, 3);
     grid_tables_kernel<<<grid, threads, 0, s>>>(
-        g, dim, cov, z1, z2, axes, ws, reinterpret_cast<float2 *>(ws + p.ey_off),
-        reinterpret_cast<float2 *>(ws + p.ez_off));
+        g, cov, z1, z2, axes, reinterpret_cast<float2 *>(ws + p.wx_off),
+        reinterpret_cast<float2 *>(ws + p.ey_off), ws + p.ez_off);
     GST_TRY_CUDA(cudaGetLastError());
     return GST_OK;
 }
@@ -606,16 +620,16 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
     if (err == nullptr) return GST_ERR_CUDA;
     GridArgs args{};
     args.g = p.g;
-    args.a_image = ws;
+    args.wx = reinterpret_cast<const float2 *>(ws + p.wx_off);
     args.ey = reinterpret_cast<const float2 *>(ws + p.ey_off);
-    args.ez = reinterpret_cast<const float2 *>(ws + p.ez_off);
+    args.ez_image = ws + p.ez_off;
     args.out = out;
     args.out_f32 = out_type == GST_OUT_F32 ? 1 : 0;
     args.scale = scale;
     args.err = err;
     const int64_t n_tiles = p.g.blocks[0] * p.g.blocks[1] * p.g.blocks[2];
     const cudaError_t e = (p.ty == 16) ? launch_grid<16>(args, n_tiles, s)
-                                       : launch_grid<kTileCols>(args, n_tiles, s);
+                                       : launch_grid<1>(args, n_tiles, s);
     GST_TRY_CUDA(e);
     return GST_OK;
 }
@@ -653,7 +667,7 @@ int gst_grid_tc_tables(int dim, int64_t n_modes, const int64_t *axis_len,
     if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
         return GST_ERR_ALIGNMENT;
     if (gst::current_device() < 0) return GST_ERR_NO_DEVICE;
-    return gst::run_tables(p, dim, axes, cov_samples, z_1, z_2,
+    return gst::run_tables(p, axes, cov_samples, z_1, z_2,
                            static_cast<unsigned char *>(workspace),
                            static_cast<cudaStream_t>(stream));
 }
@@ -707,7 +721,7 @@ int gst_summate_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,
     gst::StreamScratch ws;
     GST_TRY_CUDA(ws.alloc(p.total, s));
     unsigned char *base = static_cast<unsigned char *>(ws.ptr);
-    rc = gst::run_tables(p, dim, axes, cov_samples, z_1, z_2, base, s);
+    rc = gst::run_tables(p, axes, cov_samples, z_1, z_2, base, s);
     if (rc) return rc;
     return gst::run_contract(p, base, out, out_type, scale, s);
 }
