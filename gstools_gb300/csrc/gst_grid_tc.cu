@@ -49,18 +49,19 @@ namespace {
 
 constexpr int kThreads = 320;
 constexpr int kGenThreads = 256;      // warps 2-9
-constexpr int kTileRows = 128;        // (x, y) rows per tile (MMA M)
-constexpr int kTileCols = 256;        // z points per tile (MMA N)
+constexpr int kCtaRows = 128;         // (x, y) rows held by each CTA
+constexpr int kPairRows = 256;        // rows of one CTA pair (MMA M)
+constexpr int kTileCols = 256;        // z points per pair tile (MMA N)
+constexpr int kCtaCols = 128;         // z rows of B held by each CTA
 constexpr int kModesPerKStep = 4;     // 8 reals = K of one tf32 MMA
-constexpr int kKSteps = 2;            // K-steps per pipeline stage
-constexpr int kModesPerStage = kModesPerKStep * kKSteps;
-constexpr int kABlockBytes = kTileRows * 8 * 4;     // 128 rows x 8 tf32
-constexpr int kBBlockBytes = kTileCols * 8 * 4;     // 256 rows x 8 tf32
-constexpr int kAStageBytes = kKSteps * 2 * kABlockBytes;      // 16 KB
-constexpr int kBStageBytes = kKSteps * 2 * kBBlockBytes;      // 32 KB
+constexpr int kBlockBytes = 128 * 8 * 4;             // 128 rows x 8 tf32
 constexpr uint32_t kTmemCols = 512;  // two 256-column accumulators
-constexpr int kChunkStages = 4;      // 32 modes accumulate per chunk
+constexpr int kChunkModes = 32;      // modes accumulated per TMEM chunk
 constexpr int kColsPerThread = 128;  // epilogue: half a row of 256 columns
+
+// K-steps per pipeline stage: 4 (16 modes) for 3-D grids; 2 for 2-D grids,
+// whose per-CTA w*Ex slice (128 distinct x rows) is 16 times larger.
+__host__ __device__ constexpr int ksteps_for(int ty) { return ty == 1 ? 2 : 4; }
 
 constexpr double kInv2Pi = 0.15915494309189533576888376337251436;
 
@@ -90,27 +91,27 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
 }
 
 // Instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major,
-// M = 128, N = 256.
+// M = 256 (a CTA pair), N = 256.
 constexpr uint32_t kIdesc = (1u << 4)            // D format F32
                             | (2u << 7)          // A format TF32
                             | (2u << 10)         // B format TF32
                             | ((256u >> 3) << 17)  // N
-                            | ((128u >> 4) << 24); // M
+                            | ((256u >> 4) << 24); // M
 
 // ------------------------------------------------------------- tcgen05 ops --
 
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols) {
     asm volatile(
-        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+        "tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
             smem_addr(dst_smem)),
         "r"(ncols)
         : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::
                      : "memory");
 }
 
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(
                      taddr),
                  "r"(ncols)
                  : "memory");
@@ -124,22 +125,74 @@ __device__ __forceinline__ void tc_fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+// One M=256 x N=256 x K=8 MMA over the CTA pair, issued by the leader.
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc,
                                          uint64_t b_desc, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+        "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
             d_tmem),
         "l"(a_desc), "l"(b_desc), "r"(kIdesc), "r"(accumulate)
         : "memory");
 }
 
-__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+// Arrives on `bar` (same offset) in both CTAs of the pair once the MMAs
+// issued so far have completed.
+__device__ __forceinline__ void mma_commit_pair(uint64_t *bar) {
+    const uint16_t mask = 0x3;
     asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
-        "[%0];" ::"r"(smem_addr(bar))
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster."
+        "multicast::cluster.b64 [%0], %1;" ::"r"(smem_addr(bar)),
+        "h"(mask)
         : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+                 "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Arrive on the barrier at the same offset in CTA `rank` of the cluster.
+__device__ __forceinline__ void mbar_arrive_remote(uint64_t *bar, uint32_t rank) {
+    uint32_t remote;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(remote)
+                 : "r"(smem_addr(bar)), "r"(rank));
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(remote)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_cluster(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on a barrier that also receives arrivals from the peer CTA.
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t *bar, uint32_t parity,
+                                                  unsigned int *err) {
+    if (mbar_try_cluster(bar, parity)) return true;
+    const uint64_t t0 = global_timer_ns();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try_cluster(bar, parity)) return true;
+        if ((it & 15u) == 0u && global_timer_ns() - t0 > kWaitLimitNs) {
+            atomicOr(err, kErrWaitTimeout);
+            return false;
+        }
+    }
 }
 
 __device__ __forceinline__ void fence_async_smem() {
@@ -179,15 +232,18 @@ struct GridGeom {
     int64_t n[3];        // x, y, z lengths (2-D: y is a dummy axis of length 1)
     int64_t off[3];      // offsets of the axes in the concatenated array
     int src[3];          // caller axis feeding x, y, z (-1: dummy)
-    int64_t blocks[3];   // tiles along x (TX), y (TY), z (256)
+    int64_t blocks[3];   // table blocks along x (TX, even count), y (TY), z (256)
     int tile[3];         // TX, TY, 256 with TX * TY = 128
-    int64_t n_stages;    // padded modes / kModesPerStage
+    int64_t n_stages;    // padded modes / modes per stage
     int64_t n_modes;
+    int ksteps;          // K-steps (4 modes each) per pipeline stage
 };
 
 // One thread per (axis point, mode).  Axis x writes w*Ex, axis y writes Ey
 // (complex FP32, blocked [block][stage][mode][tile]); axis z writes the
-// pre-split TF32 image of [Re Ez, Im Ez] per 256-point block and stage.
+// pre-split TF32 image of [Re Ez, Im Ez]: per 256-point block and stage,
+// the half of each CTA of a pair (128 points) is one contiguous 16 KB run of
+// [K-step][hi, lo] blocks in the UMMA canonical K-major layout.
 __global__ void grid_tables_kernel(GridGeom g, const double *__restrict__ cov,
                                    const double *__restrict__ z1,
                                    const double *__restrict__ z2,
@@ -195,7 +251,8 @@ __global__ void grid_tables_kernel(GridGeom g, const double *__restrict__ cov,
                                    float2 *__restrict__ wx, float2 *__restrict__ ey,
                                    unsigned char *__restrict__ ez_image) {
     const int axis = blockIdx.z;
-    const int64_t n_pad_modes = g.n_stages * kModesPerStage;
+    const int mps = kModesPerKStep * g.ksteps;   // modes per stage
+    const int64_t n_pad_modes = g.n_stages * mps;
     const int64_t rows = g.blocks[axis] * g.tile[axis];
     const int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (idx >= rows * n_pad_modes) return;
@@ -216,8 +273,8 @@ __global__ void grid_tables_kernel(GridGeom g, const double *__restrict__ cov,
         const double frac = t - rint(t);
         sincospif(2.0f * static_cast<float>(frac), &s, &c);
     }
-    const int64_t st = j / kModesPerStage;
-    const int mm = static_cast<int>(j % kModesPerStage);
+    const int64_t st = j / mps;
+    const int mm = static_cast<int>(j % mps);
     const int tile = g.tile[axis];
     const int64_t blk = r / tile;
     const int t = static_cast<int>(r % tile);
@@ -229,23 +286,24 @@ __global__ void grid_tables_kernel(GridGeom g, const double *__restrict__ cov,
             re = static_cast<float>(zz1 * c + zz2 * s);
             im = static_cast<float>(zz1 * s - zz2 * c);
         }
-        wx[((blk * g.n_stages + st) * kModesPerStage + mm) * tile + t] =
-            make_float2(re, im);
+        wx[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(re, im);
     } else if (axis == 1) {
-        ey[((blk * g.n_stages + st) * kModesPerStage + mm) * tile + t] =
-            make_float2(c, s);
+        ey[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(c, s);
     } else {
+        const int rank = t / kCtaCols;
+        const uint32_t row = static_cast<uint32_t>(t % kCtaCols);
         const int kstep = mm / kModesPerKStep;
         const uint32_t k0 = 2u * (mm % kModesPerKStep);
-        unsigned char *stage = ez_image + (blk * g.n_stages + st) * kBStageBytes;
+        const int64_t half_bytes = static_cast<int64_t>(g.ksteps) * 2 * kBlockBytes;
+        unsigned char *half = ez_image + ((blk * g.n_stages + st) * 2 + rank) * half_bytes;
         const float vals[2] = {c, s};
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             const float hi = to_tf32(vals[q]);
             const float lo = to_tf32(vals[q] - hi);
-            const uint32_t o = core_offset(static_cast<uint32_t>(t), k0 + q);
-            *reinterpret_cast<float *>(stage + (kstep * 2 + 0) * kBBlockBytes + o) = hi;
-            *reinterpret_cast<float *>(stage + (kstep * 2 + 1) * kBBlockBytes + o) = lo;
+            const uint32_t o = core_offset(row, k0 + q);
+            *reinterpret_cast<float *>(half + (kstep * 2 + 0) * kBlockBytes + o) = hi;
+            *reinterpret_cast<float *>(half + (kstep * 2 + 1) * kBlockBytes + o) = lo;
         }
     }
 }
@@ -258,6 +316,7 @@ __device__ __forceinline__ int64_t ceil_div_dev(int64_t a, int64_t b) {
 
 struct GridArgs {
     GridGeom g;
+    int64_t pair_blocks[3];   // pair tiles along x (2 TX), y (TY), z (256)
     const float2 *wx;
     const float2 *ey;
     const unsigned char *ez_image;
@@ -267,27 +326,31 @@ struct GridArgs {
     unsigned int *err;
 };
 
-// Shared memory: a ring of bulk-copied slots (Ez image + w*Ex and Ey slices)
-// and a ring of generated A slots.
+// One ring of pipeline slots per CTA: its half of B (bulk copy), its w*Ex
+// and Ey table slices (bulk copies) and its 128 rows of A (generated).
 template <int TY>
 struct StageLayout {
-    static constexpr int TX = kTileRows / TY;
+    static constexpr int TX = kCtaRows / TY;
+    static constexpr int KS = ksteps_for(TY);
+    static constexpr int kModesPerStage = kModesPerKStep * KS;
+    static constexpr int kChunkStages = kChunkModes / kModesPerStage;
+    static constexpr int kAStageBytes = KS * 2 * kBlockBytes;
+    static constexpr int kBStageBytes = KS * 2 * kBlockBytes;   // per CTA
     static constexpr int kWxBytes = kModesPerStage * TX * 8;
     static constexpr int kEyBytes = kModesPerStage * TY * 8;
     static constexpr int kB = 0;
-    static constexpr int kWx = kB + kBStageBytes;
+    static constexpr int kA = kB + kBStageBytes;
+    static constexpr int kWx = kA + kAStageBytes;
     static constexpr int kEy = kWx + kWxBytes;
     static constexpr int kCopyBytes = kBStageBytes + kWxBytes + kEyBytes;
-    static constexpr int kSlotB = (kCopyBytes + 1023) / 1024 * 1024;
-    static constexpr int kSlotA = kAStageBytes;
+    static constexpr int kSlot = (kEy + kEyBytes + 1023) / 1024 * 1024;
     static constexpr int kBudget = 227 * 1024 - 2048;
-    static constexpr int kPipeA = 4;
-    static constexpr int kPipeB0 = (kBudget - kPipeA * kSlotA) / kSlotB;
-    static constexpr int kPipeB = kPipeB0 > 4 ? 4 : kPipeB0;
-    static constexpr int kRingA = kPipeB * kSlotB;
-    static constexpr int kBars = kRingA + kPipeA * kSlotA;
-    static constexpr int kSmem = kBars + 1024 /*align*/ + 256 /*bars*/;
-    static_assert(kPipeB >= 3, "copy ring too shallow");
+    static constexpr int kPipe0 = kBudget / kSlot;
+    static constexpr int kPipe = kPipe0 > 6 ? 6 : kPipe0;
+    static constexpr int kBars = kPipe * kSlot;
+    static constexpr int kSmem = kBars + 1024 /*align*/ + 512 /*bars*/;
+    static_assert(kPipe >= 3, "ring too shallow");
+    static_assert(kChunkStages >= 1, "chunk shorter than a stage");
 };
 
 template <int TY>
@@ -295,50 +358,57 @@ __global__ void __launch_bounds__(kThreads, 1)
     grid_tc_kernel(const GridArgs a) {
     using L = StageLayout<TY>;
     constexpr int TX = L::TX;
-    constexpr int PB = L::kPipeB;   // copy ring (B operand + tables)
-    constexpr int PA = L::kPipeA;   // generated ring (A operand)
+    constexpr int P = L::kPipe;
+    constexpr int KS = L::KS;
+    constexpr int kModesPerStage = L::kModesPerStage;
+    constexpr int kChunkStages = L::kChunkStages;
+    constexpr int kBStageBytes = L::kBStageBytes;
 
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::kBars);
-    uint64_t *full = bars;                 // [PB] bulk copies landed
-    uint64_t *empty = bars + PB;           // [PB] MMAs done with copy slot
-    uint64_t *aready = bars + 2 * PB;      // [PA] A generated
-    uint64_t *afree = bars + 2 * PB + PA;  // [PA] MMAs done with A slot
-    uint64_t *chunk_done = bars + 2 * PB + 2 * PA;  // [2] accumulator done
-    uint64_t *acc_free = chunk_done + 2;            // [2] accumulator drained
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_free + 2);
+    uint64_t *full = bars;               // [P] local bulk copies landed
+    uint64_t *ready = bars + P;          // [P] leader: both halves generated
+    uint64_t *empty = bars + 2 * P;      // [P] pair MMAs done with the slot
+    uint64_t *gen_done = bars + 3 * P;   // [P] peer: its half generated
+    uint64_t *chunk_done = bars + 4 * P; // [2] accumulator complete
+    uint64_t *acc_free = chunk_done + 2; // [2] leader: both CTAs drained
+    uint64_t *drained = chunk_done + 4;  // [2] peer: its half drained
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(chunk_done + 6);
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_rank();
     const GridGeom &g = a.g;
 
-    const int64_t tile = blockIdx.x;
-    const int64_t zb = tile % g.blocks[2];
-    const int64_t yb = (tile / g.blocks[2]) % g.blocks[1];
-    const int64_t xb = tile / (g.blocks[2] * g.blocks[1]);
+    const int64_t pair = blockIdx.x >> 1;
+    const int64_t zb = pair % a.pair_blocks[2];
+    const int64_t yb = (pair / a.pair_blocks[2]) % a.pair_blocks[1];
+    const int64_t xb = pair / (a.pair_blocks[2] * a.pair_blocks[1]);
+    const int64_t xblk = 2 * xb + rank;   // this CTA's TX-row table block
     const int64_t n_st = g.n_stages;
     const int64_t n_chunks = ceil_div_dev(n_st, kChunkStages);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < PB; ++s) {
+        // ready / acc_free (leader): 8 local warps + the peer's relay;
+        // gen_done / drained (peer): 8 local warps.
+        for (int s = 0; s < P; ++s) {
             mbar_init(&full[s], 1);
+            mbar_init(&ready[s], kGenThreads / 32 + 1);
             mbar_init(&empty[s], 1);
-        }
-        for (int s = 0; s < PA; ++s) {
-            mbar_init(&aready[s], kGenThreads / 32);
-            mbar_init(&afree[s], 1);
+            mbar_init(&gen_done[s], kGenThreads / 32);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&chunk_done[b], 1);
-            mbar_init(&acc_free[b], kGenThreads / 32);
+            mbar_init(&acc_free[b], kGenThreads / 32 + 1);
+            mbar_init(&drained[b], kGenThreads / 32);
         }
         fence_mbar_init();
     }
     if (warp == 1) tmem_alloc(tmem_slot, kTmemCols);
     tc_fence_before();
-    __syncthreads();
+    cluster_sync();   // barriers of both CTAs initialised, TMEM allocated
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
@@ -346,17 +416,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 0) {
         // ---------------------------------------------- bulk producer --
         if (lane == 0) {
-            const unsigned char *ez_src = a.ez_image + zb * n_st * kBStageBytes;
-            const float2 *wx_src = a.wx + xb * n_st * kModesPerStage * TX;
+            const unsigned char *ez_src =
+                a.ez_image + (zb * n_st * 2 + rank) * kBStageBytes;
+            const float2 *wx_src = a.wx + xblk * n_st * kModesPerStage * TX;
             const float2 *ey_src = a.ey + yb * n_st * kModesPerStage * TY;
             for (int64_t st = 0; st < n_st && ok; ++st) {
-                const int s = static_cast<int>(st % PB);
-                const uint32_t ph = static_cast<uint32_t>((st / PB) & 1);
+                const int s = static_cast<int>(st % P);
+                const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
                 ok = mbar_wait(&empty[s], ph ^ 1u, a.err);
                 if (!ok) break;
-                unsigned char *dst = smem + s * L::kSlotB;
+                unsigned char *dst = smem + s * L::kSlot;
                 mbar_arrive_expect_tx(&full[s], L::kCopyBytes);
-                bulk_copy_g2s(dst + L::kB, ez_src + st * kBStageBytes,
+                bulk_copy_g2s(dst + L::kB, ez_src + st * 2 * kBStageBytes,
                               kBStageBytes, &full[s]);
                 bulk_copy_g2s(dst + L::kWx, wx_src + st * kModesPerStage * TX,
                               L::kWxBytes, &full[s]);
@@ -364,52 +435,79 @@ __global__ void __launch_bounds__(kThreads, 1)
                               L::kEyBytes, &full[s]);
             }
         }
+    } else if (warp == 1 && rank == 1) {
+        // ---------------------------------------- relay (peer only) --
+        // Forwards the peer's local "half generated" and "half drained"
+        // phases to the leader's ready / acc_free barriers, so the
+        // cluster-scope release of a remote arrive is paid by this thread
+        // alone, once per phase, instead of by every generator warp.
+        if (lane == 0) {
+            int64_t st = 0, c = 0;
+            uint64_t t0 = global_timer_ns();
+            while (st < n_st || c < n_chunks) {
+                bool moved = false;
+                if (st < n_st &&
+                    mbar_test(&gen_done[st % P], static_cast<uint32_t>((st / P) & 1))) {
+                    mbar_arrive_remote(&ready[st % P], 0);
+                    ++st;
+                    moved = true;
+                }
+                if (c < n_chunks &&
+                    mbar_test(&drained[c & 1], static_cast<uint32_t>((c >> 1) & 1))) {
+                    mbar_arrive_remote(&acc_free[c & 1], 0);
+                    ++c;
+                    moved = true;
+                }
+                if (moved) {
+                    t0 = global_timer_ns();
+                } else if (global_timer_ns() - t0 > kWaitLimitNs) {
+                    atomicOr(a.err, kErrWaitTimeout);
+                    break;
+                }
+            }
+        }
     } else if (warp == 1) {
-        // ---------------------------------------------- MMA issuer --
+        // ------------------------------------ MMA issuer (leader only) --
         if (lane == 0) {
             for (int64_t st = 0; st < n_st && ok; ++st) {
-                const int sb = static_cast<int>(st % PB);
-                const uint32_t phb = static_cast<uint32_t>((st / PB) & 1);
-                const int sa = static_cast<int>(st % PA);
-                const uint32_t pha = static_cast<uint32_t>((st / PA) & 1);
+                const int s = static_cast<int>(st % P);
+                const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
                 const int64_t c = st / kChunkStages;
                 const int buf = static_cast<int>(c & 1);
                 const bool first = (st % kChunkStages) == 0;
                 if (first && c >= 2) {
-                    // accumulator reused: wait until chunk c-2 was drained
-                    ok = mbar_wait(&acc_free[buf],
-                                   static_cast<uint32_t>(((c >> 1) - 1) & 1), a.err);
+                    // accumulator reused: both CTAs must have drained c - 2
+                    ok = mbar_wait_cluster(&acc_free[buf],
+                                           static_cast<uint32_t>(((c >> 1) - 1) & 1),
+                                           a.err);
                     if (!ok) break;
                 }
-                ok = mbar_wait(&full[sb], phb, a.err) &&
-                     mbar_wait(&aready[sa], pha, a.err);
+                ok = mbar_wait_cluster(&ready[s], ph, a.err);
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t bbase = smem_addr(smem + sb * L::kSlotB + L::kB);
-                const uint32_t abase = smem_addr(smem + L::kRingA + sa * L::kSlotA);
+                const uint32_t base = smem_addr(smem + s * L::kSlot);
                 const uint32_t d = tmem + buf * 256;
 #pragma unroll
-                for (int ks = 0; ks < kKSteps; ++ks) {
-                    const uint64_t bh = smem_desc(bbase + (ks * 2 + 0) * kBBlockBytes);
-                    const uint64_t bl = smem_desc(bbase + (ks * 2 + 1) * kBBlockBytes);
-                    const uint64_t ah = smem_desc(abase + (ks * 2 + 0) * kABlockBytes);
-                    const uint64_t al = smem_desc(abase + (ks * 2 + 1) * kABlockBytes);
+                for (int ks = 0; ks < KS; ++ks) {
+                    const uint64_t bh = smem_desc(base + L::kB + (ks * 2 + 0) * kBlockBytes);
+                    const uint64_t bl = smem_desc(base + L::kB + (ks * 2 + 1) * kBlockBytes);
+                    const uint64_t ah = smem_desc(base + L::kA + (ks * 2 + 0) * kBlockBytes);
+                    const uint64_t al = smem_desc(base + L::kA + (ks * 2 + 1) * kBlockBytes);
                     const uint32_t acc = (first && ks == 0) ? 0u : 1u;
                     mma_tf32(d, ah, bh, acc);
                     mma_tf32(d, ah, bl, 1u);
                     mma_tf32(d, al, bh, 1u);
                 }
-                mma_commit(&empty[sb]);
-                mma_commit(&afree[sa]);
+                mma_commit_pair(&empty[s]);
                 if ((st % kChunkStages) == kChunkStages - 1 || st == n_st - 1)
-                    mma_commit(&chunk_done[buf]);
+                    mma_commit_pair(&chunk_done[buf]);
             }
         }
     } else {
         // ------------------------------------- A generators + epilogue --
         const int gt = threadIdx.x - 64;       // 0..255
-        const int row = gt & (kTileRows - 1);  // (x, y) row of the A tile
-        const int ks_gen = gt >> 7;            // K-step this thread fills
+        const int row = gt & (kCtaRows - 1);   // (x, y) row of this CTA's A
+        const int ks_gen = gt >> 7;            // half of the stage's K-steps
         const int xl = row / TY, yl = row % TY;
         const int q = warp & 3;                // TMEM lane quarter
         const int half = (warp - 2) >> 2;      // accumulator columns half
@@ -418,9 +516,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         float acc[kColsPerThread];
 #pragma unroll
         for (int i = 0; i < kColsPerThread; ++i) acc[i] = 0.0f;
-        int64_t drained = 0;
+        int64_t n_drained = 0;
 
-        // Adds chunk `c` (accumulator c & 1) into the registers and frees it.
+        // Adds chunk `c` (accumulator c & 1) into the registers and tells
+        // the leader this warp is done with it.
         auto drain = [&](int64_t c) -> bool {
             const int buf = static_cast<int>(c & 1);
             const bool got = __all_sync(
@@ -438,62 +537,71 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&acc_free[buf]);
+            if (lane == 0) mbar_arrive(rank == 0 ? &acc_free[buf] : &drained[buf]);
             return true;
         };
 
         for (int64_t st = 0; st < n_st && ok; ++st) {
-            const int sb = static_cast<int>(st % PB);
-            const uint32_t phb = static_cast<uint32_t>((st / PB) & 1);
-            const int sa = static_cast<int>(st % PA);
-            const uint32_t pha = static_cast<uint32_t>((st / PA) & 1);
-            ok = mbar_wait(&afree[sa], pha ^ 1u, a.err) &&
-                 mbar_wait(&full[sb], phb, a.err);
+            const int s = static_cast<int>(st % P);
+            const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
+            // full[s] of this phase implies the slot was released (empty)
+            ok = mbar_wait(&full[s], ph, a.err);
             if (__any_sync(0xffffffffu, !ok)) { ok = false; break; }
-            const unsigned char *slot = smem + sb * L::kSlotB;
+            unsigned char *slot = smem + s * L::kSlot;
             const float2 *swx = reinterpret_cast<const float2 *>(slot + L::kWx);
             const float2 *sey = reinterpret_cast<const float2 *>(slot + L::kEy);
-            float hi[8], lo[8];
 #pragma unroll
-            for (int m = 0; m < kModesPerKStep; ++m) {
-                const int mm = ks_gen * kModesPerKStep + m;
-                const float2 p = swx[mm * TX + xl];
-                const float2 e = sey[mm * TY + yl];
-                const float re = fmaf(p.x, e.x, -p.y * e.y);
-                const float im = fmaf(p.x, e.y, p.y * e.x);
-                hi[2 * m] = to_tf32(re);
-                lo[2 * m] = re - hi[2 * m];   // the MMA reads lo as TF32
-                hi[2 * m + 1] = to_tf32(-im);
-                lo[2 * m + 1] = -im - hi[2 * m + 1];
-            }
-            unsigned char *aslot = smem + L::kRingA + sa * L::kSlotA;
-            unsigned char *ah = aslot + (ks_gen * 2 + 0) * kABlockBytes;
-            unsigned char *al = aslot + (ks_gen * 2 + 1) * kABlockBytes;
+            for (int kk = 0; kk < KS / 2; ++kk) {
+                const int ksg = ks_gen * (KS / 2) + kk;   // K-step filled
+                float hi[8], lo[8];
 #pragma unroll
-            for (int kb = 0; kb < 2; ++kb) {
-                const uint32_t o = core_offset(row, kb * 4);
-                *reinterpret_cast<float4 *>(ah + o) = make_float4(
-                    hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
-                *reinterpret_cast<float4 *>(al + o) = make_float4(
-                    lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
+                for (int m = 0; m < kModesPerKStep; ++m) {
+                    const int mm = ksg * kModesPerKStep + m;
+                    const float2 p = swx[mm * TX + xl];
+                    const float2 e = sey[mm * TY + yl];
+                    const float re = fmaf(p.x, e.x, -p.y * e.y);
+                    const float im = fmaf(p.x, e.y, p.y * e.x);
+                    hi[2 * m] = to_tf32(re);
+                    lo[2 * m] = re - hi[2 * m];   // the MMA reads lo as TF32
+                    hi[2 * m + 1] = to_tf32(-im);
+                    lo[2 * m + 1] = -im - hi[2 * m + 1];
+                }
+                unsigned char *ah = slot + L::kA + (ksg * 2 + 0) * kBlockBytes;
+                unsigned char *al = slot + L::kA + (ksg * 2 + 1) * kBlockBytes;
+#pragma unroll
+                for (int kb = 0; kb < 2; ++kb) {
+                    const uint32_t o = core_offset(row, kb * 4);
+                    *reinterpret_cast<float4 *>(ah + o) = make_float4(
+                        hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
+                    *reinterpret_cast<float4 *>(al + o) = make_float4(
+                        lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
+                }
             }
             fence_async_smem();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&aready[sa]);
-            // Drain the previous chunk once the MMAs are past it: generating
-            // stage st needed the MMAs of stage st - PA to be complete.
-            if (drained < n_chunks - 1 &&
-                st == (drained + 1) * kChunkStages - 1 + PA) {
-                ok = drain(drained);
-                ++drained;
+            if (lane == 0) mbar_arrive(rank == 0 ? &ready[s] : &gen_done[s]);
+            // Drain a finished chunk as soon as the tensor cores are done
+            // with it (one per stage at most).
+            if (n_drained < n_chunks) {
+                const int buf = static_cast<int>(n_drained & 1);
+                const bool done = __shfl_sync(
+                    0xffffffffu,
+                    lane == 0 ? mbar_test(&chunk_done[buf],
+                                          static_cast<uint32_t>((n_drained >> 1) & 1))
+                              : false,
+                    0);
+                if (done) {
+                    ok = drain(n_drained);
+                    ++n_drained;
+                }
             }
         }
-        for (; drained < n_chunks && ok; ++drained) ok = drain(drained);
+        for (; n_drained < n_chunks && ok; ++n_drained) ok = drain(n_drained);
 
         if (ok) {
             // this thread's accumulator row is TMEM lane q * 32 + lane
             const int erow = q * 32 + lane;
-            const int64_t x = xb * TX + erow / TY;
+            const int64_t x = xblk * TX + erow / TY;
             const int64_t y = yb * TY + erow % TY;
             const int64_t nz = g.n[2];
             const int64_t z0 = zb * kTileCols + half * kColsPerThread;
@@ -525,8 +633,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     }
 
+    // Neither CTA may leave while its peer can still reach its shared memory
+    // (MMA operands, remote arrivals) or tensor memory.
     tc_fence_before();
-    __syncthreads();
+    cluster_sync();
     if (warp == 1) {
         __syncwarp();
         tc_fence_after();
@@ -535,18 +645,32 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 template <int TY>
-cudaError_t launch_grid(const GridArgs &args, int64_t n_tiles, cudaStream_t s) {
+cudaError_t launch_grid(const GridArgs &args, int64_t n_pairs, cudaStream_t s) {
     using L = StageLayout<TY>;
     cudaError_t e = cudaFuncSetAttribute(grid_tc_kernel<TY>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          L::kSmem);
     if (e != cudaSuccess) return e;
-    grid_tc_kernel<TY><<<static_cast<unsigned>(n_tiles), kThreads, L::kSmem, s>>>(args);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(2 * n_pairs));
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = L::kSmem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, grid_tc_kernel<TY>, args);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
 struct GridPlan {
     GridGeom g;
+    int64_t pair_blocks[3];
     int ty;
     size_t wx_off, ey_off, ez_off, total;
 };
@@ -575,20 +699,28 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
         g.off[0] = 0; g.off[1] = 0; g.off[2] = axis_len[0];
         p.ty = 1;
     }
-    g.tile[0] = kTileRows / p.ty;
+    g.tile[0] = kCtaRows / p.ty;
     g.tile[1] = p.ty;
     g.tile[2] = kTileCols;
-    for (int d = 0; d < 3; ++d) g.blocks[d] = ceil_div(g.n[d], g.tile[d]);
-    g.n_stages = ceil_div(n_modes, kModesPerStage);
+    p.pair_blocks[0] = ceil_div(g.n[0], 2 * g.tile[0]);
+    p.pair_blocks[1] = ceil_div(g.n[1], g.tile[1]);
+    p.pair_blocks[2] = ceil_div(g.n[2], g.tile[2]);
+    g.blocks[0] = 2 * p.pair_blocks[0];   // both CTAs of every pair have a block
+    g.blocks[1] = p.pair_blocks[1];
+    g.blocks[2] = p.pair_blocks[2];
+    g.ksteps = ksteps_for(p.ty);
+    const int mps = kModesPerKStep * g.ksteps;
+    g.n_stages = ceil_div(n_modes, mps);
     g.n_modes = n_modes;
-    if (g.blocks[0] * g.blocks[1] * g.blocks[2] > 0x7fffffffLL)
+    if (2 * p.pair_blocks[0] * p.pair_blocks[1] * p.pair_blocks[2] > 0x7fffffffLL)
         return GST_ERR_TOO_LARGE;
-    const size_t per_stage = kModesPerStage * sizeof(float2);
+    const size_t per_stage = mps * sizeof(float2);
     const size_t wx_bytes = static_cast<size_t>(g.blocks[0]) * g.n_stages *
                             per_stage * g.tile[0];
     const size_t ey_bytes = static_cast<size_t>(g.blocks[1]) * g.n_stages *
                             per_stage * g.tile[1];
-    const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages * kBStageBytes;
+    const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages * 2 *
+                            g.ksteps * 2 * kBlockBytes;
     p.ez_off = 0;
     p.wx_off = align_up(ez_bytes, 256);
     p.ey_off = align_up(p.wx_off + wx_bytes, 256);
@@ -600,7 +732,7 @@ int run_tables(const GridPlan &p, const double *axes, const double *cov,
                const double *z1, const double *z2, unsigned char *ws,
                cudaStream_t s) {
     const GridGeom &g = p.g;
-    const int64_t n_pad_modes = g.n_stages * kModesPerStage;
+    const int64_t n_pad_modes = g.n_stages * kModesPerKStep * g.ksteps;
     int64_t max_rows = 0;
     for (int d = 0; d < 3; ++d)
         max_rows = std::max(max_rows, g.blocks[d] * g.tile[d]);
@@ -620,6 +752,7 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
     if (err == nullptr) return GST_ERR_CUDA;
     GridArgs args{};
     args.g = p.g;
+    for (int d = 0; d < 3; ++d) args.pair_blocks[d] = p.pair_blocks[d];
     args.wx = reinterpret_cast<const float2 *>(ws + p.wx_off);
     args.ey = reinterpret_cast<const float2 *>(ws + p.ey_off);
     args.ez_image = ws + p.ez_off;
@@ -627,9 +760,9 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
     args.out_f32 = out_type == GST_OUT_F32 ? 1 : 0;
     args.scale = scale;
     args.err = err;
-    const int64_t n_tiles = p.g.blocks[0] * p.g.blocks[1] * p.g.blocks[2];
-    const cudaError_t e = (p.ty == 16) ? launch_grid<16>(args, n_tiles, s)
-                                       : launch_grid<1>(args, n_tiles, s);
+    const int64_t n_pairs = p.pair_blocks[0] * p.pair_blocks[1] * p.pair_blocks[2];
+    const cudaError_t e = (p.ty == 16) ? launch_grid<16>(args, n_pairs, s)
+                                       : launch_grid<1>(args, n_pairs, s);
     GST_TRY_CUDA(e);
     return GST_OK;
 }
