@@ -657,6 +657,11 @@ def wl_incompr(args, torch, gg, flush):
     mixed = lambda: _native.call("gst_summate_incompr_grid_mixed", 3, nm, lens,
                                  p(axes), p(d[0]), p(d[1]), p(d[2]), p(out),
                                  _native.GST_OUT_F32, scale, stream)
+    out_tc = torch.empty((3, n, n, n), dtype=torch.float32, device=dev)
+    tensor = lambda: _native.call("gst_summate_incompr_grid_tc", 3, nm, lens,
+                                  p(axes), p(d[0]), p(d[0]), p(d[1]), p(d[2]),
+                                  p(out_tc), _native.GST_OUT_F32, scale, stream)
+    ttc = _timed_events(torch, tensor, args.steps, args.warmup, flush)
     tmx = _timed_events(torch, mixed, args.steps, args.warmup, flush)
     slab = 12
     lens64 = (ctypes.c_int64 * 4)(slab, n, n, 1)
@@ -668,24 +673,29 @@ def wl_incompr(args, torch, gg, flush):
                                stream)
     t64 = _timed_events(torch, f64, 1, 1, flush)
     mixed()
+    tensor()
     got = out[:, :slab].double().cpu().numpy()
     ref = scale * out64.cpu().numpy()
     diff = got - ref
+    diff_tc = out_tc[:, :slab].double().cpu().numpy() - ref
     # divergence of the float32 field by central differences (unit spacing)
-    u = out.double()
+    u = out_tc.double()
     div = ((u[0, 2:, 1:-1, 1:-1] - u[0, :-2, 1:-1, 1:-1])
            + (u[1, 1:-1, 2:, 1:-1] - u[1, 1:-1, :-2, 1:-1])
            + (u[2, 1:-1, 1:-1, 2:] - u[2, 1:-1, 1:-1, :-2])) / 2.0
     grad_scale = ((u[0, 2:, 1:-1, 1:-1] - u[0, :-2, 1:-1, 1:-1]) / 2.0).std()
     work = nm * n ** 3
     return _line(
-        args, "gau3d_incompr_grid192_modes2000", work / tmx / 1e9, tmx,
-        "fp32 + exact turn reduction",
-        {"grid": [n] * 3, "modes": nm, "components": 3, "output": "float32"},
+        args, "gau3d_incompr_grid192_modes2000", work / ttc / 1e9, ttc,
+        "tf32x3 (fp32 accumulate)",
+        {"grid": [n] * 3, "modes": nm, "components": 3, "output": "float32",
+         "path": "tensor-core grid path, one weighted contraction per component"},
         f64_plain={"value": nm * slab * n * n / t64 / 1e9, "unit": UNIT,
                    "sample": f"{slab}x{n}x{n} slab"},
-        error_vs_fp64={"rms_sigma": float(np.sqrt(np.mean(diff ** 2))),
-                       "max_abs_sigma": float(np.max(np.abs(diff)))},
+        mixed_pointwise={"value": work / tmx / 1e9, "unit": UNIT,
+                         "rms_sigma": float(np.sqrt(np.mean(diff ** 2)))},
+        error_vs_fp64={"rms_sigma": float(np.sqrt(np.mean(diff_tc ** 2))),
+                       "max_abs_sigma": float(np.max(np.abs(diff_tc)))},
         divergence={"fd_rms_over_grad_rms": float(div.std() / grad_scale),
                     "note": "central differences, h=1; O(h^2) truncation"},
         gpu_launches=2 * args.steps)

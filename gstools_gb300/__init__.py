@@ -26,6 +26,7 @@ from .srf import SRF
 from .summator import (
     summate,
     summate_fourier,
+    summate_fourier_grid,
     summate_grid,
     summate_incompr,
     summate_incompr_grid,
@@ -50,6 +51,7 @@ __all__ = [
     "summate_fourier",
     "summate_grid",
     "summate_incompr_grid",
+    "summate_fourier_grid",
     "install",
     "uninstall",
 ]

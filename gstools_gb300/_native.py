@@ -58,6 +58,12 @@ SIGNATURES = {
                                                 _dbl, _ptr]),
     "gst_summate_grid_tc": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr, _ptr,
                                      _ptr, _ptr, _c_int, _dbl, _ptr]),
+    "gst_summate_incompr_grid_tc": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr,
+                                             _ptr, _ptr, _ptr, _ptr, _c_int,
+                                             _dbl, _ptr]),
+    "gst_summate_fourier_grid_tc": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr,
+                                             _ptr, _ptr, _ptr, _ptr, _c_int,
+                                             _dbl, _ptr]),
     "gst_grid_tc_workspace_size": (_c_int, [_c_int, _i64, _ptr,
                                             ctypes.POINTER(ctypes.c_size_t)]),
     "gst_grid_tc_tables": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr, _ptr,

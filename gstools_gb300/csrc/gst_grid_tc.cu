@@ -244,10 +244,25 @@ struct GridGeom {
 // pre-split TF32 image of [Re Ez, Im Ez]: per 256-point block and stage,
 // the half of each CTA of a pair (128 points) is one contiguous 16 KB run of
 // [K-step][hi, lo] blocks in the UMMA canonical K-major layout.
+// Per-mode real weight multiplying w = z1 - i z2 (axis x only):
+//   kWeightNone       1
+//   kWeightArray      weight[j] (summate_fourier's spectrum factor)
+//   kWeightProjector  p_c(k_j) = delta_c0 - k_cj k_0j / |k_j|^2 computed from
+//                     the unmapped wave vectors `weight` (dim, N), component c
+//                     (summate_incompr, generator.py:479-495)
+enum WeightMode { kWeightNone = 0, kWeightArray = 1, kWeightProjector = 2 };
+
+struct Weight {
+    int mode;
+    int comp;
+    int dim;
+    const double *data;
+};
+
 __global__ void grid_tables_kernel(GridGeom g, const double *__restrict__ cov,
                                    const double *__restrict__ z1,
                                    const double *__restrict__ z2,
-                                   const double *__restrict__ axes,
+                                   const double *__restrict__ axes, Weight wgt,
                                    float2 *__restrict__ wx, float2 *__restrict__ ey,
                                    unsigned char *__restrict__ ez_image) {
     const int axis = blockIdx.z;
@@ -282,7 +297,19 @@ __global__ void grid_tables_kernel(GridGeom g, const double *__restrict__ cov,
         // w E with w = z1 - i z2
         float re = 0.0f, im = 0.0f;
         if (live) {
-            const double zz1 = z1[j], zz2 = z2[j];
+            double f = 1.0;
+            if (wgt.mode == kWeightArray) {
+                f = wgt.data[j];
+            } else if (wgt.mode == kWeightProjector) {
+                double k2 = 0.0;
+                for (int d = 0; d < wgt.dim; ++d) {
+                    const double kd = wgt.data[d * g.n_modes + j];
+                    k2 += kd * kd;
+                }
+                f = (wgt.comp == 0 ? 1.0 : 0.0) -
+                    wgt.data[wgt.comp * g.n_modes + j] * wgt.data[j] / k2;
+            }
+            const double zz1 = f * z1[j], zz2 = f * z2[j];
             re = static_cast<float>(zz1 * c + zz2 * s);
             im = static_cast<float>(zz1 * s - zz2 * c);
         }
@@ -730,7 +757,7 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
 
 int run_tables(const GridPlan &p, const double *axes, const double *cov,
                const double *z1, const double *z2, unsigned char *ws,
-               cudaStream_t s) {
+               cudaStream_t s, Weight wgt = Weight{kWeightNone, 0, 0, nullptr}) {
     const GridGeom &g = p.g;
     const int64_t n_pad_modes = g.n_stages * kModesPerKStep * g.ksteps;
     int64_t max_rows = 0;
@@ -740,7 +767,7 @@ int run_tables(const GridPlan &p, const double *axes, const double *cov,
     const dim3 grid(static_cast<unsigned>(ceil_div(max_rows * n_pad_modes, threads)),
                     1, 3);
     grid_tables_kernel<<<grid, threads, 0, s>>>(
-        g, cov, z1, z2, axes, reinterpret_cast<float2 *>(ws + p.wx_off),
+        g, cov, z1, z2, axes, wgt, reinterpret_cast<float2 *>(ws + p.wx_off),
         reinterpret_cast<float2 *>(ws + p.ey_off), ws + p.ez_off);
     GST_TRY_CUDA(cudaGetLastError());
     return GST_OK;
@@ -828,6 +855,66 @@ int gst_grid_tc_contract(int dim, int64_t n_modes, const int64_t *axis_len,
         return GST_ERR_ALIGNMENT;
     return gst::run_contract(p, static_cast<const unsigned char *>(workspace),
                              out, out_type, scale, s);
+}
+
+// Shared driver of the weighted grid entry points: n_comp weighted
+// contractions into consecutive output blocks, one workspace.
+static int weighted_grid(int dim, int64_t n_modes, const int64_t *axis_len,
+                         const double *axes, const double *cov, const double *z1,
+                         const double *z2, gst::Weight wgt, int n_comp, void *out,
+                         int out_type, double scale, void *stream) {
+    if (!gst::valid_out(out_type)) return GST_ERR_INVALID_ARGUMENT;
+    gst::GridPlan p;
+    int64_t total = 0;
+    int rc = gst::make_plan(dim, n_modes, axis_len, p, total);
+    if (rc) return rc;
+    if (total == 0) return GST_OK;
+    if (out == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    if (gst::current_device() < 0) return GST_ERR_NO_DEVICE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t elem = out_type == GST_OUT_F32 ? 4 : 8;
+    if (n_modes == 0) {
+        GST_TRY_CUDA(cudaMemsetAsync(out, 0, elem * total * n_comp, s));
+        return GST_OK;
+    }
+    if (cov == nullptr || z1 == nullptr || z2 == nullptr || axes == nullptr ||
+        wgt.data == nullptr)
+        return GST_ERR_INVALID_ARGUMENT;
+    gst::StreamScratch ws;
+    GST_TRY_CUDA(ws.alloc(p.total, s));
+    unsigned char *base = static_cast<unsigned char *>(ws.ptr);
+    for (int c = 0; c < n_comp; ++c) {
+        wgt.comp = c;
+        rc = gst::run_tables(p, axes, cov, z1, z2, base, s, wgt);
+        if (rc) return rc;
+        rc = gst::run_contract(p, base,
+                               static_cast<unsigned char *>(out) + elem * total * c,
+                               out_type, scale, s);
+        if (rc) return rc;
+    }
+    return GST_OK;
+}
+
+int gst_summate_incompr_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,
+                                const double *axes, const double *cov_samples,
+                                const double *proj_cov, const double *z_1,
+                                const double *z_2, void *out, int out_type,
+                                double scale, void *stream) {
+    if (dim < 2 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
+    gst::Weight w{gst::kWeightProjector, 0, dim,
+                  proj_cov ? proj_cov : cov_samples};
+    return weighted_grid(dim, n_modes, axis_len, axes, cov_samples, z_1, z_2, w,
+                         dim, out, out_type, scale, stream);
+}
+
+int gst_summate_fourier_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,
+                                const double *axes, const double *spectrum_factor,
+                                const double *modes, const double *z_1,
+                                const double *z_2, void *out, int out_type,
+                                double scale, void *stream) {
+    gst::Weight w{gst::kWeightArray, 0, dim, spectrum_factor};
+    return weighted_grid(dim, n_modes, axis_len, axes, modes, z_1, z_2, w, 1, out,
+                         out_type, scale, stream);
 }
 
 int gst_summate_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,

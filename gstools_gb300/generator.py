@@ -254,10 +254,19 @@ class IncomprRandMeth(RandMeth):
         if self.zero_var:
             return self.mean_u * e1 + nugget
         scale = float(self.mean_u * np.sqrt(self.model.var / self._mode_no))
+        if self.precision == "mixed" and self.model.dim in (2, 3):
+            # tensor-core path: phases from M^T k, projector from k
+            cov = self.model.isometrize_matrix.T @ self._cov_sample
+            summed = summate_incompr_grid(
+                cov, self._z_1, self._z_2, axes, precision="mixed",
+                out_dtype=out_dtype, scale=scale, method="tensor",
+                proj_cov=self._cov_sample)
+            return self.mean_u * e1 + summed + nugget
         if self.model.is_isotropic:
             summed = summate_incompr_grid(
                 self._cov_sample, self._z_1, self._z_2, axes,
-                precision=self.precision, out_dtype=out_dtype, scale=scale)
+                precision=self.precision, out_dtype=out_dtype, scale=scale,
+                method="pointwise")
             return self.mean_u * e1 + summed + nugget
         # The projector needs the unmapped wave vectors: evaluate pointwise on
         # the isometrized grid.

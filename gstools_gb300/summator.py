@@ -32,6 +32,7 @@ __all__ = [
     "summate_fourier",
     "summate_grid",
     "summate_incompr_grid",
+    "summate_fourier_grid",
     "device",
 ]
 
@@ -253,18 +254,42 @@ def summate_grid(cov_samples, z_1, z_2, axes, *, precision=None,
 
 
 def summate_incompr_grid(cov_samples, z_1, z_2, axes, *, precision=None,
-                         out_dtype=None, scale=1.0):
+                         out_dtype=None, scale=1.0, method="auto",
+                         proj_cov=None):
     """``summate_incompr`` on a structured grid; output (dim, *shape).
 
-    The projector uses the wave vectors as given, so only a rotation-free,
-    isotropic map (M = identity) reproduces the reference exactly.
+    ``cov_samples`` drive the phases (multiply by ``M^T`` when the reference
+    would isometrize the grid with ``M``); the projector
+    ``p(k) = e_1 - k k_1 / |k|^2`` uses ``proj_cov`` (the unmapped wave
+    vectors; default ``cov_samples``).  ``method``: "pointwise", "tensor"
+    (mixed precision, 2-D / 3-D) or "auto" (tensor for mixed precision).
+    The pointwise kernels take the projector from ``cov_samples``, so they
+    need ``proj_cov`` to be absent or equal.
     """
     prec = config.check_precision(precision)
+    if method not in ("auto", "pointwise", "tensor"):
+        raise ValueError(f"unknown method {method!r}")
     as_torch = _is_torch(cov_samples, z_1, z_2, *axes)
     dev, cov, z1, z2, flat, lens, shape = _prepare_grid(cov_samples, z_1,
                                                         z_2, axes)
     dim, n_modes = cov.shape
     stream = _stream(dev)
+    if method == "auto":
+        method = "tensor" if (prec == "mixed" and dim in (2, 3)) else "pointwise"
+    if method == "tensor":
+        if prec != "mixed":
+            raise ValueError("the tensor-core grid path is mixed precision")
+        pc = cov if proj_cov is None else _on_device(proj_cov, dev).reshape(
+            dim, n_modes)
+        code, tdtype = _out_type(out_dtype)
+        out = torch.empty((dim,) + shape, dtype=tdtype, device=dev)
+        _native.call("gst_summate_incompr_grid_tc", dim, n_modes, lens,
+                     _p(flat), _p(cov), _p(pc), _p(z1), _p(z2), _p(out), code,
+                     float(scale), stream)
+        return _finish(out, as_torch)
+    if proj_cov is not None:
+        raise ValueError("the pointwise grid kernels take the projector from "
+                         "cov_samples; use method='tensor' for proj_cov")
     if prec == "f64":
         out = torch.empty((dim,) + shape, dtype=torch.float64, device=dev)
         _native.call("gst_summate_incompr_grid_f64", dim, n_modes, lens,
@@ -277,4 +302,24 @@ def summate_incompr_grid(cov_samples, z_1, z_2, axes, *, precision=None,
         _native.call("gst_summate_incompr_grid_mixed", dim, n_modes, lens,
                      _p(flat), _p(cov), _p(z1), _p(z2), _p(out), code,
                      float(scale), stream)
+    return _finish(out, as_torch)
+
+
+def summate_fourier_grid(spectrum_factor, modes, z_1, z_2, axes, *,
+                         out_dtype=None, scale=1.0):
+    """``summate_fourier`` on a structured grid (tensor-core path, mixed
+    precision, 2-D / 3-D); output of shape ``tuple(len(a) for a in axes)``."""
+    as_torch = _is_torch(spectrum_factor, modes, z_1, z_2, *axes)
+    dev, kk, z1, z2, flat, lens, shape = _prepare_grid(modes, z_1, z_2, axes)
+    dim, n_modes = kk.shape
+    if dim not in (2, 3):
+        raise ValueError("the tensor-core grid path needs a 2-D or 3-D grid")
+    fac = _on_device(spectrum_factor, dev).reshape(-1)
+    if fac.numel() != n_modes:
+        raise ValueError("spectrum_factor must have one value per mode")
+    code, tdtype = _out_type(out_dtype)
+    out = torch.empty(shape, dtype=tdtype, device=dev)
+    _native.call("gst_summate_fourier_grid_tc", dim, n_modes, lens, _p(flat),
+                 _p(fac), _p(kk), _p(z1), _p(z2), _p(out), code, float(scale),
+                 _stream(dev))
     return _finish(out, as_torch)

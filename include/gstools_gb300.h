@@ -193,6 +193,29 @@ int gst_summate_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,
                         const double *z_1, const double *z_2, void *out,
                         int out_type, double scale, void *stream);
 
+/* summate_incompr on a structured grid through the tensor-core path: the
+ * projector p_c(k) = delta_c0 - k_c k_0 / |k|^2 is a per-mode real weight on
+ * z_1 - i z_2, so the field is dim weighted contractions.  cov_samples are
+ * the (possibly M^T-mapped) wave vectors of the phases; proj_cov (dim, N)
+ * are the unmapped wave vectors of the projector (NULL: cov_samples).
+ * out is (dim, axis_len[0], ...).  dim 2..3.  Replaces
+ * gstools_cython.field.summate_incompr on generate_grid + isometrize. */
+int gst_summate_incompr_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,
+                                const double *axes, const double *cov_samples,
+                                const double *proj_cov, const double *z_1,
+                                const double *z_2, void *out, int out_type,
+                                double scale, void *stream);
+
+/* summate_fourier on a structured grid through the tensor-core path (the
+ * spectrum factor is the per-mode weight).  Replaces
+ * gstools_cython.field.summate_fourier (generator.py:23, :682-689) when the
+ * Fourier generator evaluates a structured mesh.  dim 2..3. */
+int gst_summate_fourier_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,
+                                const double *axes, const double *spectrum_factor,
+                                const double *modes, const double *z_1,
+                                const double *z_2, void *out, int out_type,
+                                double scale, void *stream);
+
 /* The tensor-core grid path in two steps with a caller-owned workspace, so
  * that the per-axis tables can be built once and contracted many times (and
  * each step timed on its own).  The workspace is device memory, 256-byte

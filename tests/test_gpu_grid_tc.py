@@ -95,3 +95,49 @@ def test_tc_no_device_error(cuda_lib):
     from gstools_gb300 import _native
 
     assert _native.read_device_error() == 0
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("aniso", [False, True])
+def test_tc_incompressible(cuda_lib, dim, aniso):
+    from gstools_gb300.geometric import matrix_isometrize
+
+    cov, z1, z2 = case(40 + dim + 7 * aniso, dim, 333)
+    shape = (19, 33, 21)[:dim]
+    axes = [np.arange(float(n)) * 0.9 for n in shape]
+    m = (matrix_isometrize(dim, [0.4, -0.3, 0.2][: dim * (dim - 1) // 2],
+                           [0.6, 0.8][: dim - 1]) if aniso else np.eye(dim))
+    grid = np.array(np.meshgrid(*axes, indexing="ij")).reshape(dim, -1)
+    ref = oracle.c_summate_incompr(cov, z1, z2, m @ grid).reshape((dim,) + shape)
+    got = gg.summate_incompr_grid(m.T @ cov, z1, z2, axes, precision="mixed",
+                                  method="tensor", proj_cov=cov)
+    assert got.shape == (dim,) + shape
+    rms, mx = errors(got, ref, 333)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (rms, mx)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_tc_fourier_grid(cuda_lib, dim):
+    cov, z1, z2 = case(70 + dim, dim, 257)
+    fac = np.random.RandomState(dim).uniform(0.1, 1.5, size=257)
+    shape = (23, 17, 40)[:dim]
+    axes = [np.linspace(-10.0, 30.0, n) for n in shape]
+    grid = np.array(np.meshgrid(*axes, indexing="ij")).reshape(dim, -1)
+    ref = oracle.c_summate_fourier(fac, cov, z1, z2, grid).reshape(shape)
+    got = gg.summate_fourier_grid(fac, cov, z1, z2, axes)
+    d = (got - ref) / np.sqrt(np.sum(fac ** 2))
+    assert np.sqrt(np.mean(d ** 2)) <= RMS_SIGMA
+
+
+def test_incompr_mirror_structured_mixed_matches_f64(cuda_lib):
+    """IncomprRandMeth.structured: tensor path (mixed) vs FP64 pointwise,
+    anisotropic and rotated model."""
+    model = gg.Gaussian(dim=3, var=1.0, len_scale=6.0, anis=[0.7, 0.5],
+                        angles=[0.2, 0.1, 0.3])
+    axes = [np.arange(20.0), np.arange(18.0), np.arange(22.0)]
+    f64 = gg.IncomprRandMeth(model, mode_no=500, seed=3, sampling="analytic")
+    mixed = gg.IncomprRandMeth(model, mode_no=500, seed=3, sampling="analytic",
+                               precision="mixed")
+    a = f64.structured(axes, add_nugget=False)
+    b = mixed.structured(axes, add_nugget=False)
+    assert np.sqrt(np.mean((a - b) ** 2)) <= RMS_SIGMA
