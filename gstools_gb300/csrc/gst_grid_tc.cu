@@ -43,6 +43,7 @@
 #include <algorithm>
 
 #include "gst_common.cuh"
+#include "gst_mixed.cuh"
 
 namespace gst {
 namespace {
@@ -239,11 +240,6 @@ struct GridGeom {
     int ksteps;          // K-steps (4 modes each) per pipeline stage
 };
 
-// One thread per (axis point, mode).  Axis x writes w*Ex, axis y writes Ey
-// (complex FP32, blocked [block][stage][mode][tile]); axis z writes the
-// pre-split TF32 image of [Re Ez, Im Ez]: per 256-point block and stage,
-// the half of each CTA of a pair (128 points) is one contiguous 16 KB run of
-// [K-step][hi, lo] blocks in the UMMA canonical K-major layout.
 // Per-mode real weight multiplying w = z1 - i z2 (axis x only):
 //   kWeightNone       1
 //   kWeightArray      weight[j] (summate_fourier's spectrum factor)
@@ -259,59 +255,117 @@ struct Weight {
     const double *data;
 };
 
-__global__ void grid_tables_kernel(GridGeom g, const double *__restrict__ cov,
-                                   const double *__restrict__ z1,
-                                   const double *__restrict__ z2,
-                                   const double *__restrict__ axes, Weight wgt,
+// Element `i` (0..2) of a small parameter array without dynamic indexing
+// (which would copy the kernel parameter to local memory).
+template <typename T>
+__device__ __forceinline__ T pick3(const T (&v)[3], int i) {
+    return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]);
+}
+
+// Per-mode and per-point splits for the table kernel, so that it runs in
+// FP32 only (GB300's FP64 rate is 1/64 of FP32).  Mode entry (8 floats):
+// qh[3], ql[3] of q = k / (2 pi) (12-bit head + tail, see gst_mixed.cuh) and
+// the weighted amplitudes f z1, f z2.  Point entry: xh, xl, xf, 0.
+struct ModeSplit {
+    float qh[3], ql[3], w1, w2;
+};
+
+__global__ void grid_prep_kernel(GridGeom g, const double *__restrict__ cov,
+                                 const double *__restrict__ z1,
+                                 const double *__restrict__ z2,
+                                 const double *__restrict__ axes, Weight wgt,
+                                 int64_t n_pad_modes, int64_t pt_base1,
+                                 int64_t pt_base2, int64_t n_pt_total,
+                                 ModeSplit *__restrict__ modes,
+                                 float4 *__restrict__ points) {
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i < n_pad_modes) {
+        ModeSplit m{};
+        if (i < g.n_modes) {
+            double f = 1.0;
+            if (wgt.mode == kWeightArray) {
+                f = wgt.data[i];
+            } else if (wgt.mode == kWeightProjector) {
+                double k2 = 0.0;
+                for (int d = 0; d < wgt.dim; ++d) {
+                    const double kd = wgt.data[d * g.n_modes + i];
+                    k2 += kd * kd;
+                }
+                f = (wgt.comp == 0 ? 1.0 : 0.0) -
+                    wgt.data[wgt.comp * g.n_modes + i] * wgt.data[i] / k2;
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const int src = g.src[a];
+                const double q = src >= 0 ? cov[src * g.n_modes + i] * kInv2Pi : 0.0;
+                m.qh[a] = split_hi12(q);
+                m.ql[a] = static_cast<float>(q - static_cast<double>(m.qh[a]));
+            }
+            m.w1 = static_cast<float>(f * z1[i]);
+            m.w2 = static_cast<float>(f * z2[i]);
+        }
+        modes[i] = m;
+        return;
+    }
+    const int64_t p = i - n_pad_modes;
+    if (p >= n_pt_total) return;
+    const int axis = p < pt_base1 ? 0 : (p < pt_base2 ? 1 : 2);
+    const int64_t r = p - (axis == 0 ? 0 : (axis == 1 ? pt_base1 : pt_base2));
+    double x = 0.0;
+    if (r < pick3(g.n, axis) && pick3(g.src, axis) >= 0)
+        x = axes[pick3(g.off, axis) + r];
+    const float xh = split_hi12(x);
+    points[p] = make_float4(xh, static_cast<float>(x - static_cast<double>(xh)),
+                            static_cast<float>(x), 0.0f);
+}
+
+// One thread per (axis point, mode), points fastest, FP32 only.  Axis x
+// writes w*Ex, axis y writes Ey (complex FP32, blocked
+// [block][stage][mode][tile]); axis z writes the pre-split TF32 image of
+// [Re Ez, Im Ez]: per 256-point block and stage, the half of each CTA of a
+// pair (128 points) is one contiguous run of [K-step][hi, lo] blocks in the
+// UMMA canonical K-major layout.  The phase is reduced to turns exactly
+// (gst_mixed.cuh) before the FP32 sincospi.
+__global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ modes,
+                                   const float4 *__restrict__ points,
+                                   int64_t pt_base1, int64_t pt_base2,
                                    float2 *__restrict__ wx, float2 *__restrict__ ey,
                                    unsigned char *__restrict__ ez_image) {
     const int axis = blockIdx.z;
     const int mps = kModesPerKStep * g.ksteps;   // modes per stage
     const int64_t n_pad_modes = g.n_stages * mps;
-    const int64_t rows = g.blocks[axis] * g.tile[axis];
+    const int tile = pick3(g.tile, axis);
+    const int64_t rows = pick3(g.blocks, axis) * tile;
     const int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (idx >= rows * n_pad_modes) return;
-    const int64_t j = idx % n_pad_modes;
-    const int64_t r = idx / n_pad_modes;
+    // axis points fastest: coalesced table writes, one mode per warp
+    const int64_t r = idx % rows;
+    const int64_t j = idx / rows;
 
     float c = 0.0f, s = 0.0f;
-    const bool live = (j < g.n_modes) && (r < g.n[axis]);
+    const bool live = (j < g.n_modes) && (r < pick3(g.n, axis));
+    const float *mf = reinterpret_cast<const float *>(modes + j);
+    const float w1 = mf[6], w2 = mf[7];
     if (live) {
-        const int src = g.src[axis];
-        double k = 0.0, x = 0.0;
-        if (src >= 0) {
-            k = cov[src * g.n_modes + j];
-            x = axes[g.off[axis] + r];
-        }
-        // exact reduction of the phase to turns, FP32 sin/cos of the rest
-        const double t = (k * kInv2Pi) * x;
-        const double frac = t - rint(t);
-        sincospif(2.0f * static_cast<float>(frac), &s, &c);
+        const float4 pt = points[(axis == 0 ? 0 : (axis == 1 ? pt_base1 : pt_base2)) + r];
+        MixedPoint<1> mp;
+        mp.xh[0] = pt.x;
+        mp.xl[0] = pt.y;
+        mp.xf[0] = pt.z;
+        const float qh[3] = {mf[axis], 0.0f, 0.0f};
+        const float ql[3] = {mf[3 + axis], 0.0f, 0.0f};
+        sincospif(2.0f * mixed_turns<1>(qh, ql, mp), &s, &c);
     }
     const int64_t st = j / mps;
     const int mm = static_cast<int>(j % mps);
-    const int tile = g.tile[axis];
     const int64_t blk = r / tile;
     const int t = static_cast<int>(r % tile);
     if (axis == 0) {
-        // w E with w = z1 - i z2
+        // w E with w = f (z1 - i z2)
         float re = 0.0f, im = 0.0f;
         if (live) {
-            double f = 1.0;
-            if (wgt.mode == kWeightArray) {
-                f = wgt.data[j];
-            } else if (wgt.mode == kWeightProjector) {
-                double k2 = 0.0;
-                for (int d = 0; d < wgt.dim; ++d) {
-                    const double kd = wgt.data[d * g.n_modes + j];
-                    k2 += kd * kd;
-                }
-                f = (wgt.comp == 0 ? 1.0 : 0.0) -
-                    wgt.data[wgt.comp * g.n_modes + j] * wgt.data[j] / k2;
-            }
-            const double zz1 = f * z1[j], zz2 = f * z2[j];
-            re = static_cast<float>(zz1 * c + zz2 * s);
-            im = static_cast<float>(zz1 * s - zz2 * c);
+            re = fmaf(w1, c, w2 * s);
+            im = fmaf(w1, s, -w2 * c);
         }
         wx[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(re, im);
     } else if (axis == 1) {
@@ -699,7 +753,8 @@ struct GridPlan {
     GridGeom g;
     int64_t pair_blocks[3];
     int ty;
-    size_t wx_off, ey_off, ez_off, total;
+    int64_t pt_base1, pt_base2, n_pt_total;   // point-split sections
+    size_t wx_off, ey_off, ez_off, modes_off, points_off, total;
 };
 
 int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
@@ -748,10 +803,15 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
                             per_stage * g.tile[1];
     const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages * 2 *
                             g.ksteps * 2 * kBlockBytes;
+    p.pt_base1 = g.blocks[0] * g.tile[0];
+    p.pt_base2 = p.pt_base1 + g.blocks[1] * g.tile[1];
+    p.n_pt_total = p.pt_base2 + g.blocks[2] * g.tile[2];
     p.ez_off = 0;
     p.wx_off = align_up(ez_bytes, 256);
     p.ey_off = align_up(p.wx_off + wx_bytes, 256);
-    p.total = p.ey_off + ey_bytes;
+    p.modes_off = align_up(p.ey_off + ey_bytes, 256);
+    p.points_off = align_up(p.modes_off + sizeof(ModeSplit) * g.n_stages * mps, 256);
+    p.total = p.points_off + sizeof(float4) * p.n_pt_total;
     return GST_OK;
 }
 
@@ -760,14 +820,22 @@ int run_tables(const GridPlan &p, const double *axes, const double *cov,
                cudaStream_t s, Weight wgt = Weight{kWeightNone, 0, 0, nullptr}) {
     const GridGeom &g = p.g;
     const int64_t n_pad_modes = g.n_stages * kModesPerKStep * g.ksteps;
+    ModeSplit *modes = reinterpret_cast<ModeSplit *>(ws + p.modes_off);
+    float4 *points = reinterpret_cast<float4 *>(ws + p.points_off);
+    const int threads = 256;
+    grid_prep_kernel<<<static_cast<unsigned>(ceil_div(n_pad_modes + p.n_pt_total, threads)),
+                       threads, 0, s>>>(g, cov, z1, z2, axes, wgt, n_pad_modes,
+                                        p.pt_base1, p.pt_base2, p.n_pt_total, modes,
+                                        points);
+    GST_TRY_CUDA(cudaGetLastError());
     int64_t max_rows = 0;
     for (int d = 0; d < 3; ++d)
         max_rows = std::max(max_rows, g.blocks[d] * g.tile[d]);
-    const int threads = 256;
     const dim3 grid(static_cast<unsigned>(ceil_div(max_rows * n_pad_modes, threads)),
                     1, 3);
     grid_tables_kernel<<<grid, threads, 0, s>>>(
-        g, cov, z1, z2, axes, wgt, reinterpret_cast<float2 *>(ws + p.wx_off),
+        g, modes, points, p.pt_base1, p.pt_base2,
+        reinterpret_cast<float2 *>(ws + p.wx_off),
         reinterpret_cast<float2 *>(ws + p.ey_off), ws + p.ez_off);
     GST_TRY_CUDA(cudaGetLastError());
     return GST_OK;
