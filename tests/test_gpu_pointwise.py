@@ -261,3 +261,27 @@ def test_no_device_error_recorded(cuda_lib):
     from gstools_gb300 import _native
 
     assert _native.read_device_error() == 0
+
+
+def test_hook_drives_installed_summators(cuda_lib, ref_goldens):
+    """install() on a stand-in of gstools.field.generator: the rebound
+    globals are called exactly as RandMeth.__call__ calls them
+    (generator.py:266-270) and reproduce the reference goldens."""
+    import types
+
+    mod = types.SimpleNamespace(_summate=None, _summate_incompr=None,
+                                _summate_fourier=None)
+    gg.install(mod)
+    try:
+        c = ref_goldens.case("randmeth_2d")
+        summed = mod._summate(c["cov"], c["z1"], c["z2"], c["pos"], None)
+        field = np.sqrt(c["var"] / c["cov"].shape[1]) * summed
+        for exp, idx in zip(c["expected"], c["index"]):
+            assert round(abs(field[tuple(idx)] - exp), 7) == 0
+        c = ref_goldens.case("incompr_2d")
+        summed = mod._summate_incompr(c["cov"], c["z1"], c["z2"], c["pos"], 4)
+        ref = oracle.c_summate_incompr(c["cov"], c["z1"], c["z2"], c["pos"])
+        assert rel_err(summed, ref) <= F64_REL
+    finally:
+        gg.uninstall(mod)
+    assert mod._summate is None
