@@ -398,6 +398,13 @@ __device__ __forceinline__ int64_t ceil_div_dev(int64_t a, int64_t b) {
 struct GridArgs {
     GridGeom g;
     int64_t pair_blocks[3];   // pair tiles along x (2 TX), y (TY), z (256)
+    // Work items: the first n_full pair tiles run whole; every later tile is
+    // split into `split` (1 or 2) parts over its stages, and the parts add
+    // their scaled sums into the (pre-zeroed) output, so the last partial
+    // wave of tiles is spread over the idle SM pairs.
+    int64_t n_full;
+    int split;
+    int64_t stages_per_part;
     const float2 *wx;
     const float2 *ey;
     const unsigned char *ez_image;
@@ -463,12 +470,22 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t rank = cluster_rank();
     const GridGeom &g = a.g;
 
-    const int64_t pair = blockIdx.x >> 1;
+    const int64_t item = blockIdx.x >> 1;
+    int64_t pair = item, st0 = 0, st1 = g.n_stages;
+    bool accumulate_out = false;
+    if (item >= a.n_full) {
+        const int64_t j = item - a.n_full;
+        pair = a.n_full + j / a.split;
+        st0 = (j % a.split) * a.stages_per_part;
+        st1 = min(st0 + a.stages_per_part, g.n_stages);
+        accumulate_out = a.split > 1;
+    }
     const int64_t zb = pair % a.pair_blocks[2];
     const int64_t yb = (pair / a.pair_blocks[2]) % a.pair_blocks[1];
     const int64_t xb = pair / (a.pair_blocks[2] * a.pair_blocks[1]);
     const int64_t xblk = 2 * xb + rank;   // this CTA's TX-row table block
-    const int64_t n_st = g.n_stages;
+    const int64_t n_all = g.n_stages;         // stages in the tables
+    const int64_t n_st = max(st1 - st0, int64_t(0));  // stages of this item
     const int64_t n_chunks = ceil_div_dev(n_st, kChunkStages);
 
     if (threadIdx.x == 0) {
@@ -498,9 +515,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ---------------------------------------------- bulk producer --
         if (lane == 0) {
             const unsigned char *ez_src =
-                a.ez_image + (zb * n_st * 2 + rank) * kBStageBytes;
-            const float2 *wx_src = a.wx + xblk * n_st * kModesPerStage * TX;
-            const float2 *ey_src = a.ey + yb * n_st * kModesPerStage * TY;
+                a.ez_image + ((zb * n_all + st0) * 2 + rank) * kBStageBytes;
+            const float2 *wx_src =
+                a.wx + (xblk * n_all + st0) * kModesPerStage * TX;
+            const float2 *ey_src = a.ey + (yb * n_all + st0) * kModesPerStage * TY;
             for (int64_t st = 0; st < n_st && ok; ++st) {
                 const int s = static_cast<int>(st % P);
                 const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
@@ -690,7 +708,29 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int64_t base = (x * g.n[1] + y) * nz + z0;
                 const int64_t nvalid = min(static_cast<int64_t>(kColsPerThread), nz - z0);
                 const float sc = static_cast<float>(a.scale);
-                if (a.out_f32) {
+                if (accumulate_out) {
+                    // part of a split tile: add into the zeroed output
+                    if (a.out_f32) {
+                        float *o = static_cast<float *>(a.out) + base;
+                        if (nvalid == kColsPerThread &&
+                            (reinterpret_cast<uintptr_t>(o) & 15u) == 0) {
+#pragma unroll
+                            for (int i = 0; i < kColsPerThread; i += 4)
+                                atomicAdd(reinterpret_cast<float4 *>(o + i),
+                                          make_float4(sc * acc[i], sc * acc[i + 1],
+                                                      sc * acc[i + 2], sc * acc[i + 3]));
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < kColsPerThread; ++i)
+                                if (i < nvalid) atomicAdd(o + i, sc * acc[i]);
+                        }
+                    } else {
+                        double *o = static_cast<double *>(a.out) + base;
+#pragma unroll
+                        for (int i = 0; i < kColsPerThread; ++i)
+                            if (i < nvalid) atomicAdd(o + i, a.scale * acc[i]);
+                    }
+                } else if (a.out_f32) {
                     float *o = static_cast<float *>(a.out) + base;
                     if (nvalid == kColsPerThread &&
                         (reinterpret_cast<uintptr_t>(o) & 15u) == 0) {
@@ -722,6 +762,32 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
         tc_fence_after();
         tmem_dealloc(tmem, kTmemCols);
+    }
+}
+
+// Zeroes the output of the split pair tiles (their parts add into it).
+__global__ void zero_split_tiles_kernel(GridGeom g, GridArgs a, int64_t first_tile,
+                                        int64_t n_tiles, int tx, int ty) {
+    const int64_t rows = 2 * static_cast<int64_t>(tx) * ty;
+    const int64_t total = n_tiles * rows * kTileCols;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+         i < total; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t zl = i % kTileCols;
+        const int64_t r = (i / kTileCols) % rows;
+        const int64_t pair = first_tile + i / (kTileCols * rows);
+        const int64_t zb = pair % a.pair_blocks[2];
+        const int64_t yb = (pair / a.pair_blocks[2]) % a.pair_blocks[1];
+        const int64_t xb = pair / (a.pair_blocks[2] * a.pair_blocks[1]);
+        const int64_t x = xb * 2 * tx + r / ty;
+        const int64_t y = yb * ty + r % ty;
+        const int64_t z = zb * kTileCols + zl;
+        if (x < g.n[0] && y < g.n[1] && z < g.n[2]) {
+            const int64_t o = (x * g.n[1] + y) * g.n[2] + z;
+            if (a.out_f32)
+                static_cast<float *>(a.out)[o] = 0.0f;
+            else
+                static_cast<double *>(a.out)[o] = 0.0;
+        }
     }
 }
 
@@ -855,9 +921,29 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
     args.out_f32 = out_type == GST_OUT_F32 ? 1 : 0;
     args.scale = scale;
     args.err = err;
-    const int64_t n_pairs = p.pair_blocks[0] * p.pair_blocks[1] * p.pair_blocks[2];
-    const cudaError_t e = (p.ty == 16) ? launch_grid<16>(args, n_pairs, s)
-                                       : launch_grid<1>(args, n_pairs, s);
+    const int64_t n_tiles = p.pair_blocks[0] * p.pair_blocks[1] * p.pair_blocks[2];
+    // Tiles of the last partial wave are split in two over their stages
+    // when that fits in the idle SM pairs (two parts per tile keep the sum
+    // order-independent: both add into an exact zero).
+    const int64_t slots = std::max(1, sm_count() / 2);
+    const int64_t tail = n_tiles % slots;
+    int split = 1;
+    if (tail > 0 && 2 * tail <= slots && p.g.n_stages >= 2) split = 2;
+    args.split = split;
+    args.n_full = split > 1 ? n_tiles - tail : n_tiles;
+    args.stages_per_part = ceil_div(p.g.n_stages, split);
+    if (split > 1) {
+        const int tx = p.g.tile[0], ty = p.g.tile[1];
+        const int64_t work = tail * 2 * tx * ty * kTileCols;
+        const int blocks = static_cast<int>(std::min<int64_t>(ceil_div(work, 256),
+                                                              sm_count() * 8));
+        zero_split_tiles_kernel<<<blocks, 256, 0, s>>>(p.g, args, args.n_full, tail,
+                                                       tx, ty);
+        GST_TRY_CUDA(cudaGetLastError());
+    }
+    const int64_t n_items = args.n_full + (n_tiles - args.n_full) * split;
+    const cudaError_t e = (p.ty == 16) ? launch_grid<16>(args, n_items, s)
+                                       : launch_grid<1>(args, n_items, s);
     GST_TRY_CUDA(e);
     return GST_OK;
 }
