@@ -82,6 +82,17 @@ SIGNATURES = {
     "gst_summate_vjp_modes_mixed": (_c_int, [_c_int, _i64, _i64] + [_ptr] * 9),
     "gst_summate_vjp_pos_f64": (_c_int, [_c_int, _i64, _i64] + [_ptr] * 6),
     "gst_summate_vjp_pos_mixed": (_c_int, [_c_int, _i64, _i64] + [_ptr] * 6),
+    "gst_grid_tc_contract_rows": (_c_int, [_c_int, _i64, _ptr, _ptr,
+                                           ctypes.c_size_t, _ptr, _c_int, _dbl,
+                                           _i64, _i64, _ptr]),
+    "gst_summate_grid_tc_host": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr, _ptr,
+                                          _ptr, _ptr, _c_int, _dbl, _ptr]),
+    "gst_summate_incompr_grid_tc_host": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr,
+                                                  _ptr, _ptr, _ptr, _ptr, _c_int,
+                                                  _dbl, _ptr]),
+    "gst_summate_fourier_grid_tc_host": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr,
+                                                  _ptr, _ptr, _ptr, _ptr, _c_int,
+                                                  _dbl, _ptr]),
     "gst_peak_probe": (_c_int, [_c_int, _i64, _ptr, ctypes.POINTER(_dbl),
                                 _ptr]),
 }

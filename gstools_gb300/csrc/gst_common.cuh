@@ -37,6 +37,15 @@ unsigned int *device_error_word();
 // Current device ordinal, or -1 with GST_ERR_NO_DEVICE semantics.
 int current_device();
 
+// The library's stream-ordered memory pool on the current device (created
+// on first use; it keeps up to 1 GiB of freed scratch mapped, where the
+// default pool unmaps it at every synchronisation), or null.
+cudaMemPool_t scratch_pool();
+
+// A non-blocking stream of the current device for device-to-host copies
+// that overlap the library's kernels (created on first use), or null.
+cudaStream_t copy_stream();
+
 // Stream-ordered scratch allocation that always frees on the same stream.
 struct StreamScratch {
     void *ptr = nullptr;
@@ -47,6 +56,8 @@ struct StreamScratch {
     cudaError_t alloc(size_t bytes, cudaStream_t s) {
         stream = s;
         if (bytes == 0) return cudaSuccess;
+        cudaMemPool_t pool = scratch_pool();
+        if (pool != nullptr) return cudaMallocFromPoolAsync(&ptr, bytes, pool, s);
         return cudaMallocAsync(&ptr, bytes, s);
     }
 };

@@ -41,6 +41,7 @@
 // Every mbarrier wait is bounded (gst::mbar_wait); a timeout is recorded in
 // the device error word and the CTA still frees its tensor memory.
 #include <algorithm>
+#include <cstring>
 
 #include "gst_common.cuh"
 #include "gst_mixed.cuh"
@@ -405,6 +406,7 @@ struct GridArgs {
     int64_t n_full;
     int split;
     int64_t stages_per_part;
+    int64_t tile_offset;   // first pair tile of this launch
     const float2 *wx;
     const float2 *ey;
     const unsigned char *ez_image;
@@ -480,6 +482,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         st1 = min(st0 + a.stages_per_part, g.n_stages);
         accumulate_out = a.split > 1;
     }
+    pair += a.tile_offset;
     const int64_t zb = pair % a.pair_blocks[2];
     const int64_t yb = (pair / a.pair_blocks[2]) % a.pair_blocks[1];
     const int64_t xb = pair / (a.pair_blocks[2] * a.pair_blocks[1]);
@@ -774,7 +777,7 @@ __global__ void zero_split_tiles_kernel(GridGeom g, GridArgs a, int64_t first_ti
          i < total; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int64_t zl = i % kTileCols;
         const int64_t r = (i / kTileCols) % rows;
-        const int64_t pair = first_tile + i / (kTileCols * rows);
+        const int64_t pair = a.tile_offset + first_tile + i / (kTileCols * rows);
         const int64_t zb = pair % a.pair_blocks[2];
         const int64_t yb = (pair / a.pair_blocks[2]) % a.pair_blocks[1];
         const int64_t xb = pair / (a.pair_blocks[2] * a.pair_blocks[1]);
@@ -908,7 +911,8 @@ int run_tables(const GridPlan &p, const double *axes, const double *cov,
 }
 
 int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
-                 int out_type, double scale, cudaStream_t s) {
+                 int out_type, double scale, cudaStream_t s,
+                 int64_t tile_begin = 0, int64_t tile_end = -1) {
     unsigned int *err = device_error_word();
     if (err == nullptr) return GST_ERR_CUDA;
     GridArgs args{};
@@ -921,7 +925,11 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
     args.out_f32 = out_type == GST_OUT_F32 ? 1 : 0;
     args.scale = scale;
     args.err = err;
-    const int64_t n_tiles = p.pair_blocks[0] * p.pair_blocks[1] * p.pair_blocks[2];
+    const int64_t all_tiles = p.pair_blocks[0] * p.pair_blocks[1] * p.pair_blocks[2];
+    if (tile_end < 0 || tile_end > all_tiles) tile_end = all_tiles;
+    if (tile_begin >= tile_end) return GST_OK;
+    const int64_t n_tiles = tile_end - tile_begin;
+    args.tile_offset = tile_begin;
     // Tiles of the last partial wave are split in two over their stages
     // when that fits in the idle SM pairs (two parts per tile keep the sum
     // order-independent: both add into an exact zero).
@@ -929,6 +937,13 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
     const int64_t tail = n_tiles % slots;
     int split = 1;
     if (tail > 0 && 2 * tail <= slots && p.g.n_stages >= 2) split = 2;
+    // Outputs in host memory (zero-copy over the C2C link) get plain stores
+    // only: no split tiles, hence no atomics on host memory.
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, out) == cudaSuccess &&
+        attr.type == cudaMemoryTypeHost)
+        split = 1;
+    cudaGetLastError();  // an unregistered pointer leaves an error behind
     args.split = split;
     args.n_full = split > 1 ? n_tiles - tail : n_tiles;
     args.stages_per_part = ceil_div(p.g.n_stages, split);
@@ -1049,6 +1064,148 @@ static int weighted_grid(int dim, int64_t n_modes, const int64_t *axis_len,
     return GST_OK;
 }
 
+// Host-memory variant of weighted_grid: copies the inputs in, computes every
+// component in x slabs and copies each finished slab to `out` on the
+// library's copy stream while the next slab computes.  `out` in pinned
+// memory gives asynchronous copies; the call is ordered on `stream` (the
+// output is complete once `stream` is).
+static int weighted_grid_host(int dim, int64_t n_modes, const int64_t *axis_len,
+                              const double *axes, const double *cov,
+                              const double *z1, const double *z2,
+                              gst::Weight wgt, int64_t wgt_len, int n_comp,
+                              void *out, int out_type, double scale,
+                              void *stream) {
+    if (!gst::valid_out(out_type)) return GST_ERR_INVALID_ARGUMENT;
+    gst::GridPlan p;
+    int64_t total = 0;
+    int rc = gst::make_plan(dim, n_modes, axis_len, p, total);
+    if (rc) return rc;
+    if (total == 0) return GST_OK;
+    if (out == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    if (gst::current_device() < 0) return GST_ERR_NO_DEVICE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t elem = out_type == GST_OUT_F32 ? 4 : 8;
+    const size_t comp_bytes = elem * static_cast<size_t>(total);
+    if (n_modes == 0) {
+        GST_TRY_CUDA(cudaStreamSynchronize(s));
+        memset(out, 0, comp_bytes * n_comp);
+        return GST_OK;
+    }
+    if (cov == nullptr || z1 == nullptr || z2 == nullptr || axes == nullptr ||
+        (wgt.mode != gst::kWeightNone && wgt.data == nullptr))
+        return GST_ERR_INVALID_ARGUMENT;
+    cudaStream_t cs = gst::copy_stream();
+    if (cs == nullptr) return GST_ERR_CUDA;
+    // One scratch block: inputs | tables workspace | device field.
+    int64_t n_axis = 0;
+    for (int d = 0; d < dim; ++d) n_axis += axis_len[d];
+    const int64_t n_in = n_axis + (dim + 2) * n_modes +
+                         (wgt.mode != gst::kWeightNone ? wgt_len : 0);
+    const size_t in_bytes = gst::align_up(8 * static_cast<size_t>(n_in), 256);
+    const size_t ws_bytes = gst::align_up(p.total, 256);
+    gst::StreamScratch scratch;
+    GST_TRY_CUDA(scratch.alloc(in_bytes + ws_bytes + comp_bytes * n_comp, s));
+    unsigned char *base = static_cast<unsigned char *>(scratch.ptr);
+    double *d_in = reinterpret_cast<double *>(base);
+    unsigned char *ws = base + in_bytes;
+    unsigned char *field = ws + ws_bytes;
+    double *d_axes = d_in, *d_cov = d_axes + n_axis, *d_z1 = d_cov + dim * n_modes;
+    double *d_z2 = d_z1 + n_modes, *d_w = d_z2 + n_modes;
+    GST_TRY_CUDA(cudaMemcpyAsync(d_axes, axes, 8 * n_axis, cudaMemcpyHostToDevice, s));
+    GST_TRY_CUDA(cudaMemcpyAsync(d_cov, cov, 8 * dim * n_modes,
+                                 cudaMemcpyHostToDevice, s));
+    GST_TRY_CUDA(cudaMemcpyAsync(d_z1, z1, 8 * n_modes, cudaMemcpyHostToDevice, s));
+    GST_TRY_CUDA(cudaMemcpyAsync(d_z2, z2, 8 * n_modes, cudaMemcpyHostToDevice, s));
+    if (wgt.mode != gst::kWeightNone) {
+        GST_TRY_CUDA(cudaMemcpyAsync(d_w, wgt.data, 8 * wgt_len,
+                                     cudaMemcpyHostToDevice, s));
+        wgt.data = d_w;
+    }
+    // Slabs: whole pair blocks along x; about 16 MiB each, at most 4 per
+    // component (measured on GB300 for a 64 MiB field: 4 slabs end 0.2 ms
+    // sooner than one contraction followed by one copy).
+    const int64_t xb = 2 * static_cast<int64_t>(p.g.tile[0]);
+    const int64_t x_blocks = gst::ceil_div(p.g.n[0], xb);
+    const int64_t per_x = p.pair_blocks[1] * p.pair_blocks[2];
+    const int64_t row_bytes = static_cast<int64_t>(comp_bytes) / p.g.n[0];
+    const int64_t want = std::max<int64_t>(1, static_cast<int64_t>(comp_bytes >> 24));
+    const int64_t n_slabs = std::min<int64_t>(std::min<int64_t>(want, 4), x_blocks);
+    constexpr int kMaxEvents = 3 * 4;
+    cudaEvent_t ev[kMaxEvents + 1] = {};
+    int n_ev = 0;
+    rc = GST_OK;
+    for (int c = 0; c < n_comp && rc == GST_OK; ++c) {
+        wgt.comp = c;
+        rc = gst::run_tables(p, d_axes, d_cov, d_z1, d_z2, ws, s, wgt);
+        for (int64_t k = 0; k < n_slabs && rc == GST_OK; ++k) {
+            const int64_t b0 = x_blocks * k / n_slabs, b1 = x_blocks * (k + 1) / n_slabs;
+            unsigned char *dst = field + comp_bytes * c;
+            rc = gst::run_contract(p, ws, dst, out_type, scale, s, b0 * per_x,
+                                   b1 * per_x);
+            if (rc) break;
+            const int64_t x0 = b0 * xb, x1 = std::min(b1 * xb, p.g.n[0]);
+            cudaError_t e = cudaEventCreateWithFlags(&ev[n_ev], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[n_ev], s);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev[n_ev], 0);
+            ++n_ev;
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(static_cast<unsigned char *>(out) + comp_bytes * c +
+                                        row_bytes * x0,
+                                    dst + row_bytes * x0, row_bytes * (x1 - x0),
+                                    cudaMemcpyDeviceToHost, cs);
+            if (e != cudaSuccess) {
+                gst::note_cuda_error(e);
+                rc = GST_ERR_CUDA;
+            }
+        }
+    }
+    // `stream` waits for the copies before the scratch goes back to the pool.
+    cudaError_t e = cudaEventCreateWithFlags(&ev[n_ev], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[n_ev], cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev[n_ev], 0);
+    ++n_ev;
+    for (int i = 0; i < n_ev; ++i)
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    if (e != cudaSuccess && rc == GST_OK) {
+        gst::note_cuda_error(e);
+        rc = GST_ERR_CUDA;
+    }
+    return rc;
+}
+
+int gst_summate_grid_tc_host(int dim, int64_t n_modes, const int64_t *axis_len,
+                             const double *axes, const double *cov_samples,
+                             const double *z_1, const double *z_2, void *out,
+                             int out_type, double scale, void *stream) {
+    gst::Weight w{gst::kWeightNone, 0, dim, nullptr};
+    return weighted_grid_host(dim, n_modes, axis_len, axes, cov_samples, z_1, z_2,
+                              w, 0, 1, out, out_type, scale, stream);
+}
+
+int gst_summate_incompr_grid_tc_host(int dim, int64_t n_modes,
+                                     const int64_t *axis_len, const double *axes,
+                                     const double *cov_samples,
+                                     const double *proj_cov, const double *z_1,
+                                     const double *z_2, void *out, int out_type,
+                                     double scale, void *stream) {
+    if (dim < 2 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
+    gst::Weight w{gst::kWeightProjector, 0, dim,
+                  proj_cov ? proj_cov : cov_samples};
+    return weighted_grid_host(dim, n_modes, axis_len, axes, cov_samples, z_1, z_2,
+                              w, dim * n_modes, dim, out, out_type, scale, stream);
+}
+
+int gst_summate_fourier_grid_tc_host(int dim, int64_t n_modes,
+                                     const int64_t *axis_len, const double *axes,
+                                     const double *spectrum_factor,
+                                     const double *modes, const double *z_1,
+                                     const double *z_2, void *out, int out_type,
+                                     double scale, void *stream) {
+    gst::Weight w{gst::kWeightArray, 0, dim, spectrum_factor};
+    return weighted_grid_host(dim, n_modes, axis_len, axes, modes, z_1, z_2, w,
+                              n_modes, 1, out, out_type, scale, stream);
+}
+
 int gst_summate_incompr_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,
                                 const double *axes, const double *cov_samples,
                                 const double *proj_cov, const double *z_1,
@@ -1069,6 +1226,41 @@ int gst_summate_fourier_grid_tc(int dim, int64_t n_modes, const int64_t *axis_le
     gst::Weight w{gst::kWeightArray, 0, dim, spectrum_factor};
     return weighted_grid(dim, n_modes, axis_len, axes, modes, z_1, z_2, w, 1, out,
                          out_type, scale, stream);
+}
+
+int gst_grid_tc_contract_rows(int dim, int64_t n_modes, const int64_t *axis_len,
+                              const void *workspace, size_t workspace_bytes,
+                              void *out, int out_type, double scale,
+                              int64_t x_begin, int64_t x_end, void *stream) {
+    if (!gst::valid_out(out_type)) return GST_ERR_INVALID_ARGUMENT;
+    gst::GridPlan p;
+    int64_t total = 0;
+    int rc = gst::make_plan(dim, n_modes, axis_len, p, total);
+    if (rc) return rc;
+    const int64_t xb = 2 * static_cast<int64_t>(p.g.tile[0]);   // pair x rows
+    if (x_begin < 0 || x_end < x_begin || x_end > p.g.n[0] || x_begin % xb != 0 ||
+        (x_end % xb != 0 && x_end != p.g.n[0]))
+        return GST_ERR_INVALID_ARGUMENT;
+    if (total == 0 || x_begin == x_end) return GST_OK;
+    if (out == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    if (gst::current_device() < 0) return GST_ERR_NO_DEVICE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t elem = out_type == GST_OUT_F32 ? 4 : 8;
+    const int64_t row_elems = total / p.g.n[0];
+    if (n_modes == 0) {
+        GST_TRY_CUDA(cudaMemsetAsync(static_cast<unsigned char *>(out) +
+                                         elem * row_elems * x_begin,
+                                     0, elem * row_elems * (x_end - x_begin), s));
+        return GST_OK;
+    }
+    if (workspace == nullptr || workspace_bytes < p.total)
+        return GST_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+        return GST_ERR_ALIGNMENT;
+    const int64_t per_x = p.pair_blocks[1] * p.pair_blocks[2];
+    return gst::run_contract(p, static_cast<const unsigned char *>(workspace), out,
+                             out_type, scale, s, (x_begin / xb) * per_x,
+                             gst::ceil_div(x_end, xb) * per_x);
 }
 
 int gst_summate_grid_tc(int dim, int64_t n_modes, const int64_t *axis_len,

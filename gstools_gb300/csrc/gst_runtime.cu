@@ -12,6 +12,11 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 int g_sm_count[kMaxDevices];
 unsigned int *g_error_word[kMaxDevices];
+cudaMemPool_t g_scratch_pool[kMaxDevices];
+bool g_scratch_pool_tried[kMaxDevices];
+cudaStream_t g_copy_stream[kMaxDevices];
+// Freed scratch the library's pool keeps mapped for the next call.
+constexpr uint64_t kScratchKeepBytes = 1ull << 30;
 thread_local cudaError_t g_last_cuda_error = cudaSuccess;
 
 }  // namespace
@@ -40,6 +45,43 @@ int sm_count() {
         g_sm_count[dev] = n;
     }
     return g_sm_count[dev];
+}
+
+cudaStream_t copy_stream() {
+    const int dev = current_device();
+    if (dev < 0) return nullptr;
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (g_copy_stream[dev] == nullptr) {
+        cudaStream_t st = nullptr;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        g_copy_stream[dev] = st;
+    }
+    return g_copy_stream[dev];
+}
+
+cudaMemPool_t scratch_pool() {
+    const int dev = current_device();
+    if (dev < 0) return nullptr;
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_scratch_pool_tried[dev]) {
+        g_scratch_pool_tried[dev] = true;
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
+            uint64_t keep = kScratchKeepBytes;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            g_scratch_pool[dev] = pool;
+        } else {
+            cudaGetLastError();
+        }
+    }
+    return g_scratch_pool[dev];
 }
 
 unsigned int *device_error_word() {

@@ -295,6 +295,45 @@ int gst_batch_run(int dim, int64_t n_items, const int64_t *mode_counts,
                   const double *scales, void *out, int out_type,
                   void *workspace, size_t workspace_bytes, void *stream);
 
+/* gst_grid_tc_contract restricted to the output rows x_begin <= x < x_end
+ * (first grid axis; both multiples of the 16-row pair block for 3-D grids,
+ * 256 for 2-D grids, or x_end = axis_len[0]).  Rows outside are untouched, so
+ * a caller can contract slab by slab and copy finished slabs to the host
+ * while the next one computes.  No counterpart in the reference. */
+int gst_grid_tc_contract_rows(int dim, int64_t n_modes, const int64_t *axis_len,
+                              const void *workspace, size_t workspace_bytes,
+                              void *out, int out_type, double scale,
+                              int64_t x_begin, int64_t x_end, void *stream);
+
+/* Host-buffer forms of gst_summate_grid_tc, gst_summate_incompr_grid_tc and
+ * gst_summate_fourier_grid_tc: every array argument (axes, cov_samples /
+ * modes, proj_cov, spectrum_factor, z_1, z_2) and `out` are in HOST memory,
+ * as the reference's summators take and return them
+ * (src/gstools/field/generator.py:266-268, :554-560, :682-689 call them with
+ * numpy arrays).  The call copies the inputs to the device, contracts the
+ * field in slabs along the first axis and copies each finished slab to
+ * `out` on a library-owned copy stream while the next slab computes.  The
+ * result is complete when `stream` is (synchronise it before reading
+ * `out`).  `out` in page-locked memory (cudaHostAlloc / cudaHostRegister)
+ * keeps the copies asynchronous; pageable `out` works but serialises them.
+ * The inputs may be pageable. */
+int gst_summate_grid_tc_host(int dim, int64_t n_modes, const int64_t *axis_len,
+                             const double *axes, const double *cov_samples,
+                             const double *z_1, const double *z_2, void *out,
+                             int out_type, double scale, void *stream);
+int gst_summate_incompr_grid_tc_host(int dim, int64_t n_modes,
+                                     const int64_t *axis_len, const double *axes,
+                                     const double *cov_samples,
+                                     const double *proj_cov, const double *z_1,
+                                     const double *z_2, void *out, int out_type,
+                                     double scale, void *stream);
+int gst_summate_fourier_grid_tc_host(int dim, int64_t n_modes,
+                                     const int64_t *axis_len, const double *axes,
+                                     const double *spectrum_factor,
+                                     const double *modes, const double *z_1,
+                                     const double *z_2, void *out, int out_type,
+                                     double scale, void *stream);
+
 /* ----------------------------------------------------------------------- */
 /* Diagnostics (no reference counterpart).                                  */
 /* ----------------------------------------------------------------------- */

@@ -141,3 +141,141 @@ def test_incompr_mirror_structured_mixed_matches_f64(cuda_lib):
     a = f64.structured(axes, add_nugget=False)
     b = mixed.structured(axes, add_nugget=False)
     assert np.sqrt(np.mean((a - b) ** 2)) <= RMS_SIGMA
+
+
+def test_tc_host_output_matches_device_output(cuda_lib):
+    """numpy inputs go through gst_summate_grid_tc_host (slabs copied to a
+    page-locked result while the next slab computes), torch inputs through
+    gst_summate_grid_tc; the two differ only where a partial wave's tiles are
+    split over their modes, by the FP32 rounding of the two-part sum."""
+    import torch
+
+    cov, z1, z2 = case(11, 3, 400)
+    axes = [np.arange(64.0), np.arange(96.0), np.arange(100.0)]
+    host = gg.summate_grid(cov, z1, z2, axes, precision="mixed",
+                           method="tensor", out_dtype="float32")
+    assert isinstance(host, np.ndarray) and host.nbytes >= (1 << 20)
+    dev = gg.summate_grid(torch.from_numpy(cov).cuda(), torch.from_numpy(z1).cuda(),
+                          torch.from_numpy(z2).cuda(),
+                          [torch.from_numpy(a).cuda() for a in axes],
+                          precision="mixed", method="tensor", out_dtype="float32")
+    np.testing.assert_allclose(host, dev.cpu().numpy(), rtol=0,
+                               atol=1e-5 * np.max(np.abs(host)))
+    grid = np.array(np.meshgrid(*[a[::9] for a in axes], indexing="ij")).reshape(3, -1)
+    ref = oracle.c_summate(cov, z1, z2, grid).reshape([len(a[::9]) for a in axes])
+    rms, mx = errors(host[::9, ::9, ::9], ref, 400)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA
+
+
+def _tc_workspace(lib, dim, n_modes, lens, flat, cov, z1, z2):
+    import ctypes
+
+    import torch
+
+    nb = ctypes.c_size_t()
+    assert lib.gst_grid_tc_workspace_size(dim, n_modes, lens, ctypes.byref(nb)) == 0
+    ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    p = [ctypes.c_void_p(t.data_ptr()) for t in (flat, cov, z1, z2, ws)]
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.gst_grid_tc_tables(dim, n_modes, lens, *p, nb, stream) == 0
+    return ws, nb
+
+
+@pytest.mark.parametrize("dim,shape", [(3, (100, 24, 40)), (2, (700, 90))])
+def test_tc_contract_rows(cuda_lib, dim, shape):
+    """Slab-by-slab contraction writes only its rows and, slab by slab,
+    gives the whole-grid contraction (up to split-tile rounding)."""
+    import ctypes
+
+    import torch
+
+    from gstools_gb300 import _native
+
+    n_modes = 301
+    cov, z1, z2 = case(5 + dim, dim, n_modes)
+    axes = [np.arange(float(n)) * 0.8 for n in shape]
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    flat = t(np.concatenate(axes))
+    lens = (ctypes.c_int64 * 4)(*(list(shape) + [1] * (4 - dim)))
+    ws, nb = _tc_workspace(cuda_lib, dim, n_modes, lens, flat, t(cov), t(z1), t(z2))
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    wsp = ctypes.c_void_p(ws.data_ptr())
+    full = torch.full(shape, float("nan"), dtype=torch.float32, device="cuda")
+    assert cuda_lib.gst_grid_tc_contract(dim, n_modes, lens, wsp, nb,
+                                         ctypes.c_void_p(full.data_ptr()),
+                                         _native.GST_OUT_F32, 0.5, stream) == 0
+    xb = 16 if dim == 3 else 256
+    cuts = [0, xb, 3 * xb, shape[0]] if dim == 3 else [0, 2 * xb, shape[0]]
+    part = torch.full(shape, float("nan"), dtype=torch.float32, device="cuda")
+    for k, (x0, x1) in enumerate(zip(cuts[:-1], cuts[1:])):
+        assert cuda_lib.gst_grid_tc_contract_rows(
+            dim, n_modes, lens, wsp, nb, ctypes.c_void_p(part.data_ptr()),
+            _native.GST_OUT_F32, 0.5, x0, x1, stream) == 0
+        got = part.cpu().numpy()
+        assert not np.isnan(got[:x1]).any() and np.isnan(got[x1:]).all(), k
+    ref = full.cpu().numpy()
+    np.testing.assert_allclose(got, ref, rtol=0, atol=2e-6 * np.abs(ref).max())
+    # misaligned or out-of-range rows are rejected before any launch
+    for x0, x1 in ((1, xb), (0, xb + 1), (xb, 0), (0, shape[0] + 1), (-xb, 0)):
+        if x1 == shape[0]:
+            continue
+        rc = cuda_lib.gst_grid_tc_contract_rows(
+            dim, n_modes, lens, wsp, nb, ctypes.c_void_p(part.data_ptr()),
+            _native.GST_OUT_F32, 0.5, x0, x1, stream)
+        assert rc == _native.GST_ERR_INVALID_ARGUMENT, (x0, x1)
+
+
+@pytest.mark.parametrize("kind", ["scalar", "incompr", "fourier"])
+@pytest.mark.parametrize("shape,out_dtype", [
+    ((128, 256, 256), "float32"),      # 32 MiB per component: 2 slabs
+    ((256, 128, 256), "float64"),      # 64 MiB: 4 slabs
+    ((2048, 4096), "float32"),         # 2-D, 32 MiB: 2 slabs of 1024 rows
+    ((300, 7, 33), "float64")])        # small: one slab, pageable result
+def test_tc_host_entry_points(cuda_lib, kind, shape, out_dtype):
+    """The *_grid_tc_host entry points (numpy in, numpy out) against the
+    device entry points on the same inputs, and against the oracle on a
+    subsample of the grid."""
+    import torch
+
+    dim, n_modes = len(shape), 200
+    cov, z1, z2 = case(len(kind) + dim, dim, n_modes, k_scale=0.05)
+    axes = [np.arange(float(n)) * 0.5 for n in shape]
+    fac = np.random.RandomState(3).uniform(0.2, 1.2, size=n_modes)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    if kind == "scalar":
+        host = gg.summate_grid(cov, z1, z2, axes, precision="mixed",
+                               method="tensor", out_dtype=out_dtype)
+        dev = gg.summate_grid(t(cov), t(z1), t(z2), [t(a) for a in axes],
+                              precision="mixed", method="tensor",
+                              out_dtype=out_dtype)
+    elif kind == "incompr":
+        host = gg.summate_incompr_grid(cov, z1, z2, axes, precision="mixed",
+                                       method="tensor", out_dtype=out_dtype)
+        dev = gg.summate_incompr_grid(t(cov), t(z1), t(z2), [t(a) for a in axes],
+                                      precision="mixed", method="tensor",
+                                      out_dtype=out_dtype)
+    else:
+        host = gg.summate_fourier_grid(fac, cov, z1, z2, axes,
+                                       out_dtype=out_dtype)
+        dev = gg.summate_fourier_grid(t(fac), t(cov), t(z1), t(z2),
+                                      [t(a) for a in axes], out_dtype=out_dtype)
+    assert isinstance(host, np.ndarray) and host.dtype == np.dtype(out_dtype)
+    dev = dev.cpu().numpy()
+    assert host.shape == dev.shape
+    np.testing.assert_allclose(host, dev, rtol=0,
+                               atol=2e-6 * np.abs(dev).max())
+    sub = [a[:: max(1, len(a) // 12)] for a in axes]
+    idx = np.ix_(*[np.arange(0, len(a), max(1, len(a) // 12)) for a in axes])
+    grid = np.array(np.meshgrid(*sub, indexing="ij")).reshape(dim, -1)
+    sub_shape = [len(a) for a in sub]
+    if kind == "scalar":
+        ref = oracle.c_summate(cov, z1, z2, grid).reshape(sub_shape)
+        got, norm = host[idx], np.sqrt(n_modes)
+    elif kind == "incompr":
+        ref = oracle.c_summate_incompr(cov, z1, z2, grid).reshape([dim] + sub_shape)
+        got, norm = host[(slice(None),) + idx], np.sqrt(n_modes)
+    else:
+        ref = oracle.c_summate_fourier(fac, cov, z1, z2, grid).reshape(sub_shape)
+        got, norm = host[idx], np.sqrt(np.sum(fac ** 2))
+    d = (got.astype(np.float64) - ref) / norm
+    assert np.sqrt(np.mean(d ** 2)) <= RMS_SIGMA and np.abs(d).max() <= MAX_SIGMA
