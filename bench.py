@@ -10,8 +10,8 @@ Metric: G mode*point evals/s of the fastest path at its stated error against
 the FP64 kernel, with the plain FP64 kernel's throughput reported beside it.
 
 * ``value``  -- device-resident inputs, CUDA-event timing of one step of the
-                separable tensor-core path (per-axis tables + 3xTF32
-                contraction; L2 flushed between steps);
+                separable tensor-core path (per-axis tables + 3xFP16
+                contraction, FP32 accumulation; L2 flushed between steps);
 * ``e2e``    -- the public API ``gstools_gb300.summate_grid`` called with host
                 numpy arrays: host->device copy of the modes and axes, the
                 kernels, and the device->host copy of the float32 field, all
@@ -65,6 +65,8 @@ def parse():
     p.add_argument("--path", default="auto",
                    choices=["auto", "mixed", "tensor", "f64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--operands", default="f16", choices=["f16", "tf32"],
+                   help="operand format of the tensor-core split GEMM")
     p.add_argument("--workload", default="grid",
                    choices=["grid", "points", "ensemble", "incompr", "adjoint"],
                    help="grid: the headline (3-D Exponential, 256^3, 2000 "
@@ -248,6 +250,7 @@ def run_ours(args):
     scale = float(np.sqrt(VAR / N_MODES))
     path = "tensor" if args.path == "auto" else args.path
 
+    _native.set_tc_operands(args.operands)
     d_cov = torch.from_numpy(np.ascontiguousarray(cov)).to(dev)
     d_z1 = torch.from_numpy(z1).to(dev)
     d_z2 = torch.from_numpy(z2).to(dev)
@@ -296,7 +299,8 @@ def run_ours(args):
     if path == "tensor":
         parts = [tc_tables, tc_contract]
         launches_per_step = 2
-        desc = "separable 3xTF32 tensor-core grid path (tables + contraction)"
+        desc = (f"separable 3x{args.operands.upper()} tensor-core grid path "
+                f"(tables + contraction)")
     else:
         parts = [step_mixed]
         launches_per_step = 2
@@ -354,6 +358,28 @@ def run_ours(args):
         t_mx, _ = timed([step_mixed], 3, 1)
         others["mixed_pointwise"] = world * work / max_over_ranks(
             statistics.mean(t_mx)) / 1e9
+        # the other operand format of the split GEMM, same workload
+        alt = "tf32" if args.operands == "f16" else "f16"
+        _native.set_tc_operands(alt)
+        alt_bytes = ctypes.c_size_t(0)
+        _native.call("gst_grid_tc_workspace_size", 3, N_MODES, lens,
+                     ctypes.byref(alt_bytes))
+        alt_ws = torch.empty(max(alt_bytes.value, 1), dtype=torch.uint8,
+                             device=dev)
+
+        def alt_tables():
+            _native.call("gst_grid_tc_tables", 3, N_MODES, lens, p(d_axes),
+                         p(d_cov), p(d_z1), p(d_z2), p(alt_ws), alt_bytes, sp)
+
+        def alt_contract():
+            _native.call("gst_grid_tc_contract", 3, N_MODES, lens, p(alt_ws),
+                         alt_bytes, p(out32), _native.GST_OUT_F32, scale, sp)
+
+        t_alt, _ = timed([alt_tables, alt_contract], 5, 2)
+        _native.set_tc_operands(args.operands)
+        others[f"tensor_{alt}_operands"] = world * work / max_over_ranks(
+            statistics.mean(t_alt)) / 1e9
+        del alt_ws
     slab = max(1, n // 16)
     lens64 = (ctypes.c_int64 * 4)(slab, n, n, 1)
     out64 = torch.empty((slab, n, n), dtype=torch.float64, device=dev)
@@ -414,8 +440,12 @@ def run_ours(args):
     if path == "tensor":
         peak, peak_src = tensor_peak()
         alg = 4.0 * work / t_main / 1e12
-        n_pad = -(-N_MODES // 8) * 8
-        executed = 12.0 * n_pad * (-(-n // 128) * 128) * n * n / t_main / 1e12
+        n_pad = -(-N_MODES // 16) * 16
+        executed = 12.0 * n_pad * (-(-n // 256) * 256) * n * n / t_main / 1e12
+        op_note = ("FP16 MMAs (3xFP16 split, padded), FP16 runs at the bf16 "
+                   "rate" if args.operands == "f16" else
+                   "TF32 MMAs (3xTF32 split, padded), TF32 runs at half the "
+                   "bf16 rate")
         roof = {"bound": "tensor", "achieved": alg, "peak": peak,
                 "unit": "TFLOP/s", "frac": alg / peak,
                 "traffic": TC_DRAM_BYTES_PER_LAUNCH,
@@ -427,8 +457,7 @@ def run_ours(args):
                 "note": (f"achieved = 4 algorithmic flops per mode*point "
                          f"(Re of a complex MAC) / contraction time; peak = "
                          f"{peak_src} dense bf16; the kernel executes "
-                         f"{executed:.0f} TFLOP/s of TF32 MMAs (3xTF32 "
-                         f"split, padded), TF32 runs at half the bf16 rate")}
+                         f"{executed:.0f} TFLOP/s of {op_note}")}
     else:
         alg = 10.0 * work / t_main / 1e12
         roof = {"bound": "fp32", "achieved": alg, "peak": peaks["fp32_tflops"],
@@ -447,7 +476,7 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": ("tf32x3 (fp32 accumulate)" if path == "tensor"
+        "dtype": (f"{args.operands}x3 (fp32 accumulate)" if path == "tensor"
                   else "fp32 + exact turn reduction"),
         "data": "synthetic (modes from the reference RNG, fixture)",
         "config": {
@@ -692,7 +721,7 @@ def wl_incompr(args, torch, gg, flush):
     work = nm * n ** 3
     return _line(
         args, "gau3d_incompr_grid192_modes2000", work / ttc / 1e9, ttc,
-        "tf32x3 (fp32 accumulate)",
+        "f16x3 (fp32 accumulate)",
         {"grid": [n] * 3, "modes": nm, "components": 3, "output": "float32",
          "path": "tensor-core grid path, one weighted contraction per component"},
         f64_plain={"value": nm * slab * n * n / t64 / 1e9, "unit": UNIT,

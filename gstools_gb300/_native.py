@@ -22,6 +22,8 @@ GST_ERR_TOO_LARGE = 7
 
 GST_OUT_F64 = 0
 GST_OUT_F32 = 1
+GST_TC_TF32 = 0
+GST_TC_F16 = 1
 
 _c_int = ctypes.c_int
 _i64 = ctypes.c_int64
@@ -93,6 +95,7 @@ SIGNATURES = {
     "gst_summate_fourier_grid_tc_host": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr,
                                                   _ptr, _ptr, _ptr, _ptr, _c_int,
                                                   _dbl, _ptr]),
+    "gst_grid_tc_set_operands": (_c_int, [_c_int]),
     "gst_peak_probe": (_c_int, [_c_int, _i64, _ptr, ctypes.POINTER(_dbl),
                                 _ptr]),
 }
@@ -154,6 +157,18 @@ def call(name, *args):
             detail = f"cudaError {load().gst_last_cuda_error()}"
         raise NativeError(name, rc, detail)
     return rc
+
+
+_TC_KINDS = {"tf32": GST_TC_TF32, "f16": GST_TC_F16}
+
+
+def set_tc_operands(kind):
+    """Select the operand format of the tensor-core grid path ("f16", the
+    default, or "tf32"; process-wide) and return the previous one."""
+    if kind not in _TC_KINDS:
+        raise ValueError(f"unknown operand kind {kind!r}; use 'f16' or 'tf32'")
+    prev = load().gst_grid_tc_set_operands(_TC_KINDS[kind])
+    return {v: k for k, v in _TC_KINDS.items()}[prev]
 
 
 def read_device_error(stream=0):

@@ -127,6 +127,21 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
+// try_wait with a suspend-time hint: the thread sleeps in hardware for up
+// to about `hint_ns` while the phase is incomplete.
+__device__ __forceinline__ bool mbar_try_hint(uint64_t *bar, uint32_t parity,
+                                              uint32_t hint_ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return ok != 0;
+}
+
 // Waits for `parity` of `bar`; gives up after kWaitLimitNs, records the
 // timeout in *err and returns false.  try_wait suspends the thread in
 // hardware between checks, so waiting warps do not steal issue slots.

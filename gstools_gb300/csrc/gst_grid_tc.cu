@@ -40,7 +40,10 @@
 //               vector stores.
 // Every mbarrier wait is bounded (gst::mbar_wait); a timeout is recorded in
 // the device error word and the CTA still frees its tensor memory.
+#include <cuda_fp16.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 
 #include "gst_common.cuh"
@@ -49,30 +52,50 @@
 namespace gst {
 namespace {
 
-constexpr int kThreads = 320;
-constexpr int kGenThreads = 256;      // warps 2-9
+constexpr int kThreads = 576;
+constexpr int kGenThreads = 512;      // warps 2-17
 constexpr int kCtaRows = 128;         // (x, y) rows held by each CTA
 constexpr int kPairRows = 256;        // rows of one CTA pair (MMA M)
 constexpr int kTileCols = 256;        // z points per pair tile (MMA N)
 constexpr int kCtaCols = 128;         // z rows of B held by each CTA
-constexpr int kModesPerKStep = 4;     // 8 reals = K of one tf32 MMA
-constexpr int kBlockBytes = 128 * 8 * 4;             // 128 rows x 8 tf32
+constexpr int kBlockBytes = 128 * 32;  // 128 rows x 32 bytes of K (one K-step)
 constexpr uint32_t kTmemCols = 512;  // two 256-column accumulators
-constexpr int kChunkModes = 32;      // modes accumulated per TMEM chunk
-constexpr int kColsPerThread = 128;  // epilogue: half a row of 256 columns
+constexpr int kColsPerThread = 64;   // epilogue: a quarter row of 256 columns
 
-// K-steps per pipeline stage: 4 (16 modes) for 3-D grids; 2 for 2-D grids,
-// whose per-CTA w*Ex slice (128 distinct x rows) is 16 times larger.
-__host__ __device__ constexpr int ksteps_for(int ty) { return ty == 1 ? 2 : 4; }
+// Operand kinds of the split GEMM.  Both carry 10 explicit mantissa bits, so
+// the three-product split (hi*hi + hi*lo + lo*hi) has the same precision;
+// FP16 products run at twice the TF32 rate and move half the bytes, but need
+// the amplitudes normalised into FP16 range (a power of two taken out of
+// w = z1 - i z2 and put back in the epilogue).
+enum OperandKind { kOpTf32 = GST_TC_TF32, kOpF16 = GST_TC_F16 };
+
+// Modes per pipeline stage: 16 for 3-D grids; 8 for 2-D grids, whose
+// per-CTA w*Ex slice (128 distinct x rows) is 16 times larger.
+__host__ __device__ constexpr int modes_per_stage(int ty) { return ty == 1 ? 8 : 16; }
+// Modes per MMA K-step (32 bytes of K per row: 8 TF32 or 16 FP16 reals).
+__host__ __device__ constexpr int modes_per_kstep(int op) { return op == kOpF16 ? 8 : 4; }
+__host__ __device__ constexpr int ksteps_for(int ty, int op) {
+    return modes_per_stage(ty) / modes_per_kstep(op);
+}
+__host__ __device__ constexpr int elem_bytes(int op) { return op == kOpF16 ? 2 : 4; }
+// Modes accumulated per TMEM chunk before the epilogue warps add the chunk
+// into FP32 registers: 24 MMAs of K = 32 bytes per chunk (32 TF32 or 64
+// FP16 modes), which keeps the tensor core's accumulation error below
+// 1e-6 sigma of the field.
+__host__ __device__ constexpr int chunk_modes(int op) { return op == kOpF16 ? 64 : 32; }
 
 constexpr double kInv2Pi = 0.15915494309189533576888376337251436;
 
 // Byte offset of element (row, k) inside one canonical K-major block of
-// 8-row x 16-byte core matrices: core (row/8, k/4) sits at
-// (row/8) * SBO + (k/4) * LBO with LBO = 128 B, SBO = 256 B.
-__host__ __device__ constexpr uint32_t core_offset(uint32_t row, uint32_t k) {
-    return (row >> 3) * 256u + (k >> 2) * 128u + (row & 7u) * 16u + (k & 3u) * 4u;
+// 8-row x 16-byte core matrices: core (row/8, k/E) sits at
+// (row/8) * SBO + (k/E) * LBO with LBO = 128 B, SBO = 256 B, E = 16 bytes /
+// element size.
+__host__ __device__ constexpr uint32_t core_offset(uint32_t row, uint32_t k, int op) {
+    return (row >> 3) * 256u + (k / (16u / elem_bytes(op))) * 128u + (row & 7u) * 16u +
+           (k % (16u / elem_bytes(op))) * elem_bytes(op);
 }
+
+std::atomic<int> g_operand_kind{kOpF16};
 
 __device__ __forceinline__ float to_tf32(float v) {
     uint32_t r;
@@ -92,13 +115,18 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
     return d;                                                    // swizzle 0
 }
 
-// Instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major,
-// M = 256 (a CTA pair), N = 256.
-constexpr uint32_t kIdesc = (1u << 4)            // D format F32
-                            | (2u << 7)          // A format TF32
-                            | (2u << 10)         // B format TF32
-                            | ((256u >> 3) << 17)  // N
-                            | ((256u >> 4) << 24); // M
+// Instruction descriptors, D = F32, A and B K-major, M = 256 (a CTA pair),
+// N = 256: kind::tf32 with A = B = TF32, kind::f16 with A = B = F16.
+constexpr uint32_t kIdescTf32 = (1u << 4)            // D format F32
+                                | (2u << 7)          // A format TF32
+                                | (2u << 10)         // B format TF32
+                                | ((256u >> 3) << 17)  // N
+                                | ((256u >> 4) << 24); // M
+constexpr uint32_t kIdescF16 = (1u << 4)             // D format F32
+                               | (0u << 7)           // A format F16
+                               | (0u << 10)          // B format F16
+                               | ((256u >> 3) << 17)   // N
+                               | ((256u >> 4) << 24);  // M
 
 // ------------------------------------------------------------- tcgen05 ops --
 
@@ -127,16 +155,35 @@ __device__ __forceinline__ void tc_fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// One M=256 x N=256 x K=8 MMA over the CTA pair, issued by the leader.
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc,
+// One M=256 x N=256 MMA over the CTA pair (K = 8 TF32 or 16 FP16 reals),
+// issued by the leader.
+template <int OP>
+__device__ __forceinline__ void mma_pair(uint32_t d_tmem, uint64_t a_desc,
                                          uint64_t b_desc, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
-            d_tmem),
-        "l"(a_desc), "l"(b_desc), "r"(kIdesc), "r"(accumulate)
-        : "memory");
+    if constexpr (OP == kOpF16) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                d_tmem),
+            "l"(a_desc), "l"(b_desc), "r"(kIdescF16), "r"(accumulate)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                d_tmem),
+            "l"(a_desc), "l"(b_desc), "r"(kIdescTf32), "r"(accumulate)
+            : "memory");
+    }
+}
+
+// hi + lo split of v in the operand format.  TF32: lo is left in FP32 (the
+// MMA reads its TF32 part).  FP16: both parts rounded to nearest.
+__device__ __forceinline__ uint32_t pack_f16x2(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&h);
 }
 
 // Arrives on `bar` (same offset) in both CTAs of the pair once the MMAs
@@ -206,6 +253,24 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
                  : "memory");
 }
 
+// 32 lanes x 16 consecutive FP32 columns of tensor memory.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]),
+          "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+          "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // 32 lanes x 32 consecutive FP32 columns of tensor memory.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     uint32_t r[32];
@@ -238,7 +303,8 @@ struct GridGeom {
     int tile[3];         // TX, TY, 256 with TX * TY = 128
     int64_t n_stages;    // padded modes / modes per stage
     int64_t n_modes;
-    int ksteps;          // K-steps (4 modes each) per pipeline stage
+    int ksteps;          // MMA K-steps per pipeline stage
+    int op;              // OperandKind
 };
 
 // Per-mode real weight multiplying w = z1 - i z2 (axis x only):
@@ -278,7 +344,8 @@ __global__ void grid_prep_kernel(GridGeom g, const double *__restrict__ cov,
                                  int64_t n_pad_modes, int64_t pt_base1,
                                  int64_t pt_base2, int64_t n_pt_total,
                                  ModeSplit *__restrict__ modes,
-                                 float4 *__restrict__ points) {
+                                 float4 *__restrict__ points,
+                                 unsigned int *__restrict__ amp_max) {
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i < n_pad_modes) {
         ModeSplit m{};
@@ -304,6 +371,8 @@ __global__ void grid_prep_kernel(GridGeom g, const double *__restrict__ cov,
             }
             m.w1 = static_cast<float>(f * z1[i]);
             m.w2 = static_cast<float>(f * z2[i]);
+            // largest amplitude (non-negative floats order like their bits)
+            atomicMax(amp_max, __float_as_uint(fmaxf(fabsf(m.w1), fabsf(m.w2))));
         }
         modes[i] = m;
         return;
@@ -320,20 +389,31 @@ __global__ void grid_prep_kernel(GridGeom g, const double *__restrict__ cov,
                             static_cast<float>(x), 0.0f);
 }
 
+// 2^-e with amp = m 2^e, m in [0.5, 1): scales the amplitudes below 1.
+__device__ __forceinline__ int amp_exponent(const unsigned int *amp_max) {
+    int e = 0;
+    frexpf(__uint_as_float(*amp_max), &e);
+    return e;
+}
+
 // One thread per (axis point, mode), points fastest, FP32 only.  Axis x
-// writes w*Ex, axis y writes Ey (complex FP32, blocked
-// [block][stage][mode][tile]); axis z writes the pre-split TF32 image of
-// [Re Ez, Im Ez]: per 256-point block and stage, the half of each CTA of a
-// pair (128 points) is one contiguous run of [K-step][hi, lo] blocks in the
-// UMMA canonical K-major layout.  The phase is reduced to turns exactly
-// (gst_mixed.cuh) before the FP32 sincospi.
+// writes w*Ex * 2^-e (amplitudes normalised below 1), axis y writes Ey
+// (complex FP32, blocked [block][stage][mode][tile]); axis z writes the
+// pre-split image of [Re Ez, Im Ez] in the operand format: per 256-point
+// block and stage, the half of each CTA of a pair (128 points) is one
+// contiguous run of [K-step][hi, lo] blocks in the UMMA canonical K-major
+// layout.  The phase is reduced to turns exactly (gst_mixed.cuh) before the
+// FP32 sincospi.
+template <int OP>
 __global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ modes,
                                    const float4 *__restrict__ points,
                                    int64_t pt_base1, int64_t pt_base2,
+                                   const unsigned int *__restrict__ amp_max,
                                    float2 *__restrict__ wx, float2 *__restrict__ ey,
                                    unsigned char *__restrict__ ez_image) {
+    constexpr int kMpk = modes_per_kstep(OP);
     const int axis = blockIdx.z;
-    const int mps = kModesPerKStep * g.ksteps;   // modes per stage
+    const int mps = kMpk * g.ksteps;   // modes per stage
     const int64_t n_pad_modes = g.n_stages * mps;
     const int tile = pick3(g.tile, axis);
     const int64_t rows = pick3(g.blocks, axis) * tile;
@@ -362,11 +442,12 @@ __global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ mod
     const int64_t blk = r / tile;
     const int t = static_cast<int>(r % tile);
     if (axis == 0) {
-        // w E with w = f (z1 - i z2)
+        // w E with w = f (z1 - i z2), times 2^-e (exact)
         float re = 0.0f, im = 0.0f;
         if (live) {
-            re = fmaf(w1, c, w2 * s);
-            im = fmaf(w1, s, -w2 * c);
+            const int e = amp_exponent(amp_max);
+            re = ldexpf(fmaf(w1, c, w2 * s), -e);
+            im = ldexpf(fmaf(w1, s, -w2 * c), -e);
         }
         wx[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(re, im);
     } else if (axis == 1) {
@@ -374,18 +455,29 @@ __global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ mod
     } else {
         const int rank = t / kCtaCols;
         const uint32_t row = static_cast<uint32_t>(t % kCtaCols);
-        const int kstep = mm / kModesPerKStep;
-        const uint32_t k0 = 2u * (mm % kModesPerKStep);
+        const int kstep = mm / kMpk;
+        const uint32_t k0 = 2u * (mm % kMpk);
         const int64_t half_bytes = static_cast<int64_t>(g.ksteps) * 2 * kBlockBytes;
         unsigned char *half = ez_image + ((blk * g.n_stages + st) * 2 + rank) * half_bytes;
-        const float vals[2] = {c, s};
+        unsigned char *bh = half + (kstep * 2 + 0) * kBlockBytes;
+        unsigned char *bl = half + (kstep * 2 + 1) * kBlockBytes;
+        if constexpr (OP == kOpF16) {
+            // (Re, Im) are adjacent in K: one 4-byte store per part
+            const __half2 hi = __floats2half2_rn(c, s);
+            const float2 hf = __half22float2(hi);
+            const uint32_t o = core_offset(row, k0, OP);
+            *reinterpret_cast<__half2 *>(bh + o) = hi;
+            *reinterpret_cast<__half2 *>(bl + o) = __floats2half2_rn(c - hf.x, s - hf.y);
+        } else {
+            const float vals[2] = {c, s};
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const float hi = to_tf32(vals[q]);
-            const float lo = to_tf32(vals[q] - hi);
-            const uint32_t o = core_offset(row, k0 + q);
-            *reinterpret_cast<float *>(half + (kstep * 2 + 0) * kBlockBytes + o) = hi;
-            *reinterpret_cast<float *>(half + (kstep * 2 + 1) * kBlockBytes + o) = lo;
+            for (int q = 0; q < 2; ++q) {
+                const float hi = to_tf32(vals[q]);
+                const float lo = to_tf32(vals[q] - hi);
+                const uint32_t o = core_offset(row, k0 + q, OP);
+                *reinterpret_cast<float *>(bh + o) = hi;
+                *reinterpret_cast<float *>(bl + o) = lo;
+            }
         }
     }
 }
@@ -410,6 +502,7 @@ struct GridArgs {
     const float2 *wx;
     const float2 *ey;
     const unsigned char *ez_image;
+    const unsigned int *amp_max;   // largest |f z|: output scaled by 2^e
     void *out;
     int out_f32;
     double scale;
@@ -418,12 +511,12 @@ struct GridArgs {
 
 // One ring of pipeline slots per CTA: its half of B (bulk copy), its w*Ex
 // and Ey table slices (bulk copies) and its 128 rows of A (generated).
-template <int TY>
+template <int TY, int OP>
 struct StageLayout {
     static constexpr int TX = kCtaRows / TY;
-    static constexpr int KS = ksteps_for(TY);
-    static constexpr int kModesPerStage = kModesPerKStep * KS;
-    static constexpr int kChunkStages = kChunkModes / kModesPerStage;
+    static constexpr int KS = ksteps_for(TY, OP);
+    static constexpr int kModesPerStage = modes_per_stage(TY);
+    static constexpr int kChunkStages = chunk_modes(OP) / kModesPerStage;
     static constexpr int kAStageBytes = KS * 2 * kBlockBytes;
     static constexpr int kBStageBytes = KS * 2 * kBlockBytes;   // per CTA
     static constexpr int kWxBytes = kModesPerStage * TX * 8;
@@ -440,13 +533,15 @@ struct StageLayout {
     static constexpr int kBars = kPipe * kSlot;
     static constexpr int kSmem = kBars + 1024 /*align*/ + 512 /*bars*/;
     static_assert(kPipe >= 3, "ring too shallow");
+    static_assert(kPipe * kSlot >= kCtaRows * (kTileCols + 4) * 4,
+                  "ring too small to stage a float32 tile");
     static_assert(kChunkStages >= 1, "chunk shorter than a stage");
 };
 
-template <int TY>
+template <int TY, int OP>
 __global__ void __launch_bounds__(kThreads, 1)
     grid_tc_kernel(const GridArgs a) {
-    using L = StageLayout<TY>;
+    using L = StageLayout<TY, OP>;
     constexpr int TX = L::TX;
     constexpr int P = L::kPipe;
     constexpr int KS = L::KS;
@@ -514,9 +609,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t tmem = *tmem_slot;
 
     bool ok = true;
+    // The three single-thread roles run as whole warps: every lane waits,
+    // lane 0 issues.  (A warp whose lane 0 loops alone while its other lanes
+    // wait to reconverge was measured to slow the generator warps of its
+    // SM sub-partition by half.)
     if (warp == 0) {
         // ---------------------------------------------- bulk producer --
-        if (lane == 0) {
+        {
             const unsigned char *ez_src =
                 a.ez_image + ((zb * n_all + st0) * 2 + rank) * kBStageBytes;
             const float2 *wx_src =
@@ -525,16 +624,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int64_t st = 0; st < n_st && ok; ++st) {
                 const int s = static_cast<int>(st % P);
                 const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
-                ok = mbar_wait(&empty[s], ph ^ 1u, a.err);
+                ok = __shfl_sync(0xffffffffu, mbar_wait(&empty[s], ph ^ 1u, a.err), 0);
                 if (!ok) break;
-                unsigned char *dst = smem + s * L::kSlot;
-                mbar_arrive_expect_tx(&full[s], L::kCopyBytes);
-                bulk_copy_g2s(dst + L::kB, ez_src + st * 2 * kBStageBytes,
-                              kBStageBytes, &full[s]);
-                bulk_copy_g2s(dst + L::kWx, wx_src + st * kModesPerStage * TX,
-                              L::kWxBytes, &full[s]);
-                bulk_copy_g2s(dst + L::kEy, ey_src + st * kModesPerStage * TY,
-                              L::kEyBytes, &full[s]);
+                if (lane == 0) {
+                    unsigned char *dst = smem + s * L::kSlot;
+                    mbar_arrive_expect_tx(&full[s], L::kCopyBytes);
+                    bulk_copy_g2s(dst + L::kB, ez_src + st * 2 * kBStageBytes,
+                                  kBStageBytes, &full[s]);
+                    bulk_copy_g2s(dst + L::kWx, wx_src + st * kModesPerStage * TX,
+                                  L::kWxBytes, &full[s]);
+                    bulk_copy_g2s(dst + L::kEy, ey_src + st * kModesPerStage * TY,
+                                  L::kEyBytes, &full[s]);
+                }
+                __syncwarp();
             }
         }
     } else if (warp == 1 && rank == 1) {
@@ -543,34 +645,64 @@ __global__ void __launch_bounds__(kThreads, 1)
         // phases to the leader's ready / acc_free barriers, so the
         // cluster-scope release of a remote arrive is paid by this thread
         // alone, once per phase, instead of by every generator warp.
-        if (lane == 0) {
+        // The thread sleeps in try_wait (suspend hint) on the next stage, or
+        // once every stage is forwarded on the next chunk, instead of
+        // spinning on test_wait beside the generator warps of its SM
+        // partition.
+        {
             int64_t st = 0, c = 0;
             uint64_t t0 = global_timer_ns();
             while (st < n_st || c < n_chunks) {
                 bool moved = false;
-                if (st < n_st &&
-                    mbar_test(&gen_done[st % P], static_cast<uint32_t>((st / P) & 1))) {
-                    mbar_arrive_remote(&ready[st % P], 0);
-                    ++st;
-                    moved = true;
+                if (st < n_st) {
+                    const bool got = __shfl_sync(
+                        0xffffffffu,
+                        mbar_try_hint(&gen_done[st % P],
+                                      static_cast<uint32_t>((st / P) & 1), 200u),
+                        0);
+                    if (got) {
+                        if (lane == 0) mbar_arrive_remote(&ready[st % P], 0);
+                        ++st;
+                        moved = true;
+                    }
+                } else {
+                    const bool got = __shfl_sync(
+                        0xffffffffu,
+                        mbar_try_hint(&drained[c & 1],
+                                      static_cast<uint32_t>((c >> 1) & 1), 200u),
+                        0);
+                    if (got) {
+                        if (lane == 0) mbar_arrive_remote(&acc_free[c & 1], 0);
+                        ++c;
+                        moved = true;
+                    }
                 }
                 if (c < n_chunks &&
-                    mbar_test(&drained[c & 1], static_cast<uint32_t>((c >> 1) & 1))) {
-                    mbar_arrive_remote(&acc_free[c & 1], 0);
+                    __shfl_sync(0xffffffffu,
+                                mbar_test(&drained[c & 1],
+                                          static_cast<uint32_t>((c >> 1) & 1)),
+                                0)) {
+                    if (lane == 0) mbar_arrive_remote(&acc_free[c & 1], 0);
                     ++c;
                     moved = true;
                 }
+                __syncwarp();
                 if (moved) {
                     t0 = global_timer_ns();
-                } else if (global_timer_ns() - t0 > kWaitLimitNs) {
-                    atomicOr(a.err, kErrWaitTimeout);
+                } else if (__shfl_sync(0xffffffffu, global_timer_ns() - t0 > kWaitLimitNs,
+                                       0)) {
+                    if (lane == 0) atomicOr(a.err, kErrWaitTimeout);
                     break;
                 }
             }
         }
     } else if (warp == 1) {
         // ------------------------------------ MMA issuer (leader only) --
-        if (lane == 0) {
+        {
+            // Descriptor of the ring's first byte; the start-address field
+            // (bits 0-13, address / 16) of any operand block is this plus
+            // its offset / 16 (shared memory < 256 KB, so it cannot carry).
+            const uint64_t desc0 = smem_desc(smem_addr(smem));
             for (int64_t st = 0; st < n_st && ok; ++st) {
                 const int s = static_cast<int>(st % P);
                 const uint32_t ph = static_cast<uint32_t>((st / P) & 1);
@@ -579,42 +711,48 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const bool first = (st % kChunkStages) == 0;
                 if (first && c >= 2) {
                     // accumulator reused: both CTAs must have drained c - 2
-                    ok = mbar_wait_cluster(&acc_free[buf],
-                                           static_cast<uint32_t>(((c >> 1) - 1) & 1),
-                                           a.err);
+                    ok = __shfl_sync(0xffffffffu,
+                                     mbar_wait_cluster(&acc_free[buf],
+                                                       static_cast<uint32_t>(
+                                                           ((c >> 1) - 1) & 1),
+                                                       a.err),
+                                     0);
                     if (!ok) break;
                 }
-                ok = mbar_wait_cluster(&ready[s], ph, a.err);
+                ok = __shfl_sync(0xffffffffu, mbar_wait_cluster(&ready[s], ph, a.err), 0);
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t base = smem_addr(smem + s * L::kSlot);
-                const uint32_t d = tmem + buf * 256;
+                if (lane == 0) {
+                    const uint64_t slot_desc = desc0 + ((s * L::kSlot) >> 4);
+                    const uint32_t d = tmem + buf * 256;
 #pragma unroll
-                for (int ks = 0; ks < KS; ++ks) {
-                    const uint64_t bh = smem_desc(base + L::kB + (ks * 2 + 0) * kBlockBytes);
-                    const uint64_t bl = smem_desc(base + L::kB + (ks * 2 + 1) * kBlockBytes);
-                    const uint64_t ah = smem_desc(base + L::kA + (ks * 2 + 0) * kBlockBytes);
-                    const uint64_t al = smem_desc(base + L::kA + (ks * 2 + 1) * kBlockBytes);
-                    const uint32_t acc = (first && ks == 0) ? 0u : 1u;
-                    mma_tf32(d, ah, bh, acc);
-                    mma_tf32(d, ah, bl, 1u);
-                    mma_tf32(d, al, bh, 1u);
+                    for (int ks = 0; ks < KS; ++ks) {
+                        const uint64_t bh = slot_desc + ((L::kB + (ks * 2 + 0) * kBlockBytes) >> 4);
+                        const uint64_t bl = slot_desc + ((L::kB + (ks * 2 + 1) * kBlockBytes) >> 4);
+                        const uint64_t ah = slot_desc + ((L::kA + (ks * 2 + 0) * kBlockBytes) >> 4);
+                        const uint64_t al = slot_desc + ((L::kA + (ks * 2 + 1) * kBlockBytes) >> 4);
+                        const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+                        mma_pair<OP>(d, ah, bh, acc);
+                        mma_pair<OP>(d, ah, bl, 1u);
+                        mma_pair<OP>(d, al, bh, 1u);
+                    }
+                    mma_commit_pair(&empty[s]);
+                    if ((st % kChunkStages) == kChunkStages - 1 || st == n_st - 1)
+                        mma_commit_pair(&chunk_done[buf]);
                 }
-                mma_commit_pair(&empty[s]);
-                if ((st % kChunkStages) == kChunkStages - 1 || st == n_st - 1)
-                    mma_commit_pair(&chunk_done[buf]);
+                __syncwarp();
             }
         }
     } else {
         // ------------------------------------- A generators + epilogue --
-        const int gt = threadIdx.x - 64;       // 0..255
+        const int gt = threadIdx.x - 64;       // 0..511
         const int row = gt & (kCtaRows - 1);   // (x, y) row of this CTA's A
-        const int ks_gen = gt >> 7;            // half of the stage's K-steps
+        const int part = gt >> 7;              // quarter of the stage's modes
         const int xl = row / TY, yl = row % TY;
         const int q = warp & 3;                // TMEM lane quarter
-        const int half = (warp - 2) >> 2;      // accumulator columns half
+        const int cq = (warp - 2) >> 2;        // accumulator column quarter
         const uint32_t t_row = tmem + (static_cast<uint32_t>(q * 32) << 16) +
-                               half * kColsPerThread;
+                               cq * kColsPerThread;
         float acc[kColsPerThread];
 #pragma unroll
         for (int i = 0; i < kColsPerThread; ++i) acc[i] = 0.0f;
@@ -631,11 +769,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (!got) return false;
             tc_fence_after();
 #pragma unroll
-            for (int j = 0; j < kColsPerThread / 32; ++j) {
-                float v[32];
-                tmem_ld32(t_row + buf * 256 + j * 32, v);
+            for (int j = 0; j < kColsPerThread / 16; ++j) {
+                float v[16];
+                tmem_ld16(t_row + buf * 256 + j * 16, v);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) acc[j * 32 + i] += v[i];
+                for (int i = 0; i < 16; ++i) acc[j * 16 + i] += v[i];
             }
             tc_fence_before();
             __syncwarp();
@@ -652,31 +790,55 @@ __global__ void __launch_bounds__(kThreads, 1)
             unsigned char *slot = smem + s * L::kSlot;
             const float2 *swx = reinterpret_cast<const float2 *>(slot + L::kWx);
             const float2 *sey = reinterpret_cast<const float2 *>(slot + L::kEy);
+            // This thread's modes: m0 .. m0 + kMpt - 1 of the stage, i.e.
+            // 2 kMpt consecutive reals [Re P, -Im P] of its row of A, stored
+            // in runs of kRun reals (at most one 16-byte core-matrix row).
+            constexpr int kMpt = kModesPerStage / (kGenThreads / kCtaRows);
+            constexpr int kMpk = modes_per_kstep(OP);
+            constexpr int kEps = 16 / elem_bytes(OP);    // reals per 16 bytes
+            constexpr int kRun = 2 * kMpt < kEps ? 2 * kMpt : kEps;
+            const int m0 = part * kMpt;
 #pragma unroll
-            for (int kk = 0; kk < KS / 2; ++kk) {
-                const int ksg = ks_gen * (KS / 2) + kk;   // K-step filled
-                float hi[8], lo[8];
+            for (int sg = 0; sg < 2 * kMpt / kRun; ++sg) {
+                const int mm = m0 + sg * kRun / 2;        // first mode of the run
+                float x[kRun];
 #pragma unroll
-                for (int m = 0; m < kModesPerKStep; ++m) {
-                    const int mm = ksg * kModesPerKStep + m;
-                    const float2 p = swx[mm * TX + xl];
-                    const float2 e = sey[mm * TY + yl];
-                    const float re = fmaf(p.x, e.x, -p.y * e.y);
-                    const float im = fmaf(p.x, e.y, p.y * e.x);
-                    hi[2 * m] = to_tf32(re);
-                    lo[2 * m] = re - hi[2 * m];   // the MMA reads lo as TF32
-                    hi[2 * m + 1] = to_tf32(-im);
-                    lo[2 * m + 1] = -im - hi[2 * m + 1];
+                for (int m = 0; m < kRun / 2; ++m) {
+                    const float2 p = swx[(mm + m) * TX + xl];
+                    const float2 e = sey[(mm + m) * TY + yl];
+                    x[2 * m] = fmaf(p.x, e.x, -p.y * e.y);
+                    x[2 * m + 1] = -fmaf(p.x, e.y, p.y * e.x);
                 }
-                unsigned char *ah = slot + L::kA + (ksg * 2 + 0) * kBlockBytes;
-                unsigned char *al = slot + L::kA + (ksg * 2 + 1) * kBlockBytes;
+                const int ksg = mm / kMpk;                // its K-step
+                const uint32_t o = core_offset(row, 2u * (mm % kMpk), OP);
+                unsigned char *ah = slot + L::kA + (ksg * 2 + 0) * kBlockBytes + o;
+                unsigned char *al = slot + L::kA + (ksg * 2 + 1) * kBlockBytes + o;
+                if constexpr (OP == kOpF16) {
+                    uint32_t h[kRun / 2], l[kRun / 2];
 #pragma unroll
-                for (int kb = 0; kb < 2; ++kb) {
-                    const uint32_t o = core_offset(row, kb * 4);
-                    *reinterpret_cast<float4 *>(ah + o) = make_float4(
-                        hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
-                    *reinterpret_cast<float4 *>(al + o) = make_float4(
-                        lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
+                    for (int i = 0; i < kRun / 2; ++i) {
+                        const __half2 hh = __floats2half2_rn(x[2 * i], x[2 * i + 1]);
+                        const float2 hf = __half22float2(hh);
+                        h[i] = *reinterpret_cast<const uint32_t *>(&hh);
+                        l[i] = pack_f16x2(x[2 * i] - hf.x, x[2 * i + 1] - hf.y);
+                    }
+                    if constexpr (kRun == 8) {
+                        *reinterpret_cast<uint4 *>(ah) = make_uint4(h[0], h[1], h[2], h[3]);
+                        *reinterpret_cast<uint4 *>(al) = make_uint4(l[0], l[1], l[2], l[3]);
+                    } else {
+                        *reinterpret_cast<uint2 *>(ah) = make_uint2(h[0], h[1]);
+                        *reinterpret_cast<uint2 *>(al) = make_uint2(l[0], l[1]);
+                    }
+                } else {
+                    static_assert(OP == kOpF16 || kRun == 4, "TF32 runs are 16 bytes");
+                    float hi[4], lo[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        hi[i] = to_tf32(x[i]);
+                        lo[i] = x[i] - hi[i];   // the MMA reads lo as TF32
+                    }
+                    *reinterpret_cast<float4 *>(ah) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                    *reinterpret_cast<float4 *>(al) = make_float4(lo[0], lo[1], lo[2], lo[3]);
                 }
             }
             fence_async_smem();
@@ -700,17 +862,58 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (; n_drained < n_chunks && ok; ++n_drained) ok = drain(n_drained);
 
-        if (ok) {
+        // Whole float32 tiles leave through shared memory: every thread
+        // parks its 64 sums (row q*32+lane, column quarter cq) in the ring,
+        // which is idle once the last chunk is drained (all MMAs that read
+        // it are complete, all copies consumed), then each warp writes
+        // 512 contiguous bytes of one row per store instead of 32 pieces of
+        // 16 bytes in 32 rows.  The condition is uniform over the CTA, and
+        // every generator thread reaches both barriers (also after a
+        // timeout), so the named barrier cannot hang.
+        const int64_t nz_all = g.n[2];
+        const bool staged = a.out_f32 && !accumulate_out &&
+                            (zb + 1) * kTileCols <= nz_all && (nz_all & 3) == 0 &&
+                            (reinterpret_cast<uintptr_t>(a.out) & 15u) == 0;
+        if (staged) {
+            constexpr int kStride = kTileCols + 4;   // floats; conflict-free float4
+            float *stage = reinterpret_cast<float *>(smem);
+            const float sc = static_cast<float>(ldexp(a.scale, amp_exponent(a.amp_max)));
+            if (ok) {
+                float *dst = stage + (q * 32 + lane) * kStride + cq * kColsPerThread;
+#pragma unroll
+                for (int i = 0; i < kColsPerThread; i += 4)
+                    *reinterpret_cast<float4 *>(dst + i) =
+                        make_float4(sc * acc[i], sc * acc[i + 1], sc * acc[i + 2],
+                                    sc * acc[i + 3]);
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(kGenThreads) : "memory");
+            constexpr int kF4PerRow = kTileCols / 4;            // 64
+            constexpr int kRowsPerPass = kGenThreads / kF4PerRow; // 8
+            const int c4 = gt % kF4PerRow;
+#pragma unroll 4
+            for (int r = gt / kF4PerRow; r < kCtaRows; r += kRowsPerPass) {
+                const int64_t x = xblk * TX + r / TY;
+                const int64_t y = yb * TY + r % TY;
+                if (x < g.n[0] && y < g.n[1]) {
+                    float *o = static_cast<float *>(a.out) + (x * g.n[1] + y) * nz_all +
+                               zb * kTileCols;
+                    reinterpret_cast<float4 *>(o)[c4] =
+                        *reinterpret_cast<const float4 *>(stage + r * kStride + 4 * c4);
+                }
+            }
+        } else if (ok) {
             // this thread's accumulator row is TMEM lane q * 32 + lane
             const int erow = q * 32 + lane;
             const int64_t x = xblk * TX + erow / TY;
             const int64_t y = yb * TY + erow % TY;
             const int64_t nz = g.n[2];
-            const int64_t z0 = zb * kTileCols + half * kColsPerThread;
+            const int64_t z0 = zb * kTileCols + cq * kColsPerThread;
             if (x < g.n[0] && y < g.n[1] && z0 < nz) {
                 const int64_t base = (x * g.n[1] + y) * nz + z0;
                 const int64_t nvalid = min(static_cast<int64_t>(kColsPerThread), nz - z0);
-                const float sc = static_cast<float>(a.scale);
+                // undo the amplitude normalisation of the tables (2^e, exact)
+                const double scale = ldexp(a.scale, amp_exponent(a.amp_max));
+                const float sc = static_cast<float>(scale);
                 if (accumulate_out) {
                     // part of a split tile: add into the zeroed output
                     if (a.out_f32) {
@@ -731,7 +934,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                         double *o = static_cast<double *>(a.out) + base;
 #pragma unroll
                         for (int i = 0; i < kColsPerThread; ++i)
-                            if (i < nvalid) atomicAdd(o + i, a.scale * acc[i]);
+                            if (i < nvalid) atomicAdd(o + i, scale * acc[i]);
                     }
                 } else if (a.out_f32) {
                     float *o = static_cast<float *>(a.out) + base;
@@ -751,7 +954,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     double *o = static_cast<double *>(a.out) + base;
 #pragma unroll
                     for (int i = 0; i < kColsPerThread; ++i)
-                        if (i < nvalid) o[i] = a.scale * acc[i];
+                        if (i < nvalid) o[i] = scale * acc[i];
                 }
             }
         }
@@ -794,10 +997,10 @@ __global__ void zero_split_tiles_kernel(GridGeom g, GridArgs a, int64_t first_ti
     }
 }
 
-template <int TY>
+template <int TY, int OP>
 cudaError_t launch_grid(const GridArgs &args, int64_t n_pairs, cudaStream_t s) {
-    using L = StageLayout<TY>;
-    cudaError_t e = cudaFuncSetAttribute(grid_tc_kernel<TY>,
+    using L = StageLayout<TY, OP>;
+    cudaError_t e = cudaFuncSetAttribute(grid_tc_kernel<TY, OP>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          L::kSmem);
     if (e != cudaSuccess) return e;
@@ -813,7 +1016,7 @@ cudaError_t launch_grid(const GridArgs &args, int64_t n_pairs, cudaStream_t s) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, grid_tc_kernel<TY>, args);
+    e = cudaLaunchKernelEx(&cfg, grid_tc_kernel<TY, OP>, args);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
@@ -823,11 +1026,11 @@ struct GridPlan {
     int64_t pair_blocks[3];
     int ty;
     int64_t pt_base1, pt_base2, n_pt_total;   // point-split sections
-    size_t wx_off, ey_off, ez_off, modes_off, points_off, total;
+    size_t wx_off, ey_off, ez_off, modes_off, points_off, amp_off, total;
 };
 
 int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
-              int64_t &total_pts) {
+              int64_t &total_pts, int op = g_operand_kind.load()) {
     if (dim < 2 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
     if (axis_len == nullptr || n_modes < 0) return GST_ERR_INVALID_ARGUMENT;
     GridGeom &g = p.g;
@@ -859,8 +1062,9 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
     g.blocks[0] = 2 * p.pair_blocks[0];   // both CTAs of every pair have a block
     g.blocks[1] = p.pair_blocks[1];
     g.blocks[2] = p.pair_blocks[2];
-    g.ksteps = ksteps_for(p.ty);
-    const int mps = kModesPerKStep * g.ksteps;
+    g.op = op;
+    g.ksteps = ksteps_for(p.ty, op);
+    const int mps = modes_per_stage(p.ty);
     g.n_stages = ceil_div(n_modes, mps);
     g.n_modes = n_modes;
     if (2 * p.pair_blocks[0] * p.pair_blocks[1] * p.pair_blocks[2] > 0x7fffffffLL)
@@ -880,7 +1084,8 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
     p.ey_off = align_up(p.wx_off + wx_bytes, 256);
     p.modes_off = align_up(p.ey_off + ey_bytes, 256);
     p.points_off = align_up(p.modes_off + sizeof(ModeSplit) * g.n_stages * mps, 256);
-    p.total = p.points_off + sizeof(float4) * p.n_pt_total;
+    p.amp_off = align_up(p.points_off + sizeof(float4) * p.n_pt_total, 256);
+    p.total = p.amp_off + sizeof(unsigned int);
     return GST_OK;
 }
 
@@ -888,24 +1093,28 @@ int run_tables(const GridPlan &p, const double *axes, const double *cov,
                const double *z1, const double *z2, unsigned char *ws,
                cudaStream_t s, Weight wgt = Weight{kWeightNone, 0, 0, nullptr}) {
     const GridGeom &g = p.g;
-    const int64_t n_pad_modes = g.n_stages * kModesPerKStep * g.ksteps;
+    const int64_t n_pad_modes = g.n_stages * modes_per_stage(p.ty);
     ModeSplit *modes = reinterpret_cast<ModeSplit *>(ws + p.modes_off);
     float4 *points = reinterpret_cast<float4 *>(ws + p.points_off);
+    unsigned int *amp = reinterpret_cast<unsigned int *>(ws + p.amp_off);
     const int threads = 256;
+    GST_TRY_CUDA(cudaMemsetAsync(amp, 0, sizeof(unsigned int), s));
     grid_prep_kernel<<<static_cast<unsigned>(ceil_div(n_pad_modes + p.n_pt_total, threads)),
                        threads, 0, s>>>(g, cov, z1, z2, axes, wgt, n_pad_modes,
                                         p.pt_base1, p.pt_base2, p.n_pt_total, modes,
-                                        points);
+                                        points, amp);
     GST_TRY_CUDA(cudaGetLastError());
     int64_t max_rows = 0;
     for (int d = 0; d < 3; ++d)
         max_rows = std::max(max_rows, g.blocks[d] * g.tile[d]);
     const dim3 grid(static_cast<unsigned>(ceil_div(max_rows * n_pad_modes, threads)),
                     1, 3);
-    grid_tables_kernel<<<grid, threads, 0, s>>>(
-        g, modes, points, p.pt_base1, p.pt_base2,
-        reinterpret_cast<float2 *>(ws + p.wx_off),
-        reinterpret_cast<float2 *>(ws + p.ey_off), ws + p.ez_off);
+    auto *tables = g.op == kOpF16 ? grid_tables_kernel<kOpF16>
+                                  : grid_tables_kernel<kOpTf32>;
+    tables<<<grid, threads, 0, s>>>(g, modes, points, p.pt_base1, p.pt_base2, amp,
+                                    reinterpret_cast<float2 *>(ws + p.wx_off),
+                                    reinterpret_cast<float2 *>(ws + p.ey_off),
+                                    ws + p.ez_off);
     GST_TRY_CUDA(cudaGetLastError());
     return GST_OK;
 }
@@ -921,6 +1130,7 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
     args.wx = reinterpret_cast<const float2 *>(ws + p.wx_off);
     args.ey = reinterpret_cast<const float2 *>(ws + p.ey_off);
     args.ez_image = ws + p.ez_off;
+    args.amp_max = reinterpret_cast<const unsigned int *>(ws + p.amp_off);
     args.out = out;
     args.out_f32 = out_type == GST_OUT_F32 ? 1 : 0;
     args.scale = scale;
@@ -957,8 +1167,13 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
         GST_TRY_CUDA(cudaGetLastError());
     }
     const int64_t n_items = args.n_full + (n_tiles - args.n_full) * split;
-    const cudaError_t e = (p.ty == 16) ? launch_grid<16>(args, n_items, s)
-                                       : launch_grid<1>(args, n_items, s);
+    cudaError_t e;
+    if (p.g.op == kOpF16)
+        e = (p.ty == 16) ? launch_grid<16, kOpF16>(args, n_items, s)
+                         : launch_grid<1, kOpF16>(args, n_items, s);
+    else
+        e = (p.ty == 16) ? launch_grid<16, kOpTf32>(args, n_items, s)
+                         : launch_grid<1, kOpTf32>(args, n_items, s);
     GST_TRY_CUDA(e);
     return GST_OK;
 }
@@ -969,6 +1184,11 @@ bool valid_out(int t) { return t == GST_OUT_F64 || t == GST_OUT_F32; }
 }  // namespace gst
 
 extern "C" {
+
+int gst_grid_tc_set_operands(int kind) {
+    if (kind != GST_TC_TF32 && kind != GST_TC_F16) return -1;
+    return gst::g_operand_kind.exchange(kind);
+}
 
 int gst_grid_tc_workspace_size(int dim, int64_t n_modes,
                                const int64_t *axis_len, size_t *bytes) {

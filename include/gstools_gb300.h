@@ -295,6 +295,17 @@ int gst_batch_run(int dim, int64_t n_items, const int64_t *mode_counts,
                   const double *scales, void *out, int out_type,
                   void *workspace, size_t workspace_bytes, void *stream);
 
+/* Operand format of the tensor-core grid path's split GEMM (hi*hi + hi*lo +
+ * lo*hi): GST_TC_F16 (default; FP16 products at twice the TF32 rate, the
+ * amplitudes normalised by a power of two) or GST_TC_TF32.  Both keep 10
+ * explicit mantissa bits per part.  Process-wide; returns the previous kind
+ * (or -1 for an unknown kind, leaving it unchanged).  A workspace filled by
+ * gst_grid_tc_tables must be contracted under the kind it was filled with.
+ * No counterpart in the reference. */
+#define GST_TC_TF32 0
+#define GST_TC_F16 1
+int gst_grid_tc_set_operands(int kind);
+
 /* gst_grid_tc_contract restricted to the output rows x_begin <= x < x_end
  * (first grid axis; both multiples of the 16-row pair block for 3-D grids,
  * 256 for 2-D grids, or x_end = axis_len[0]).  Rows outside are untouched, so

@@ -52,3 +52,16 @@ def test_library_is_the_in_tree_build(lib):
     assert os.path.dirname(_native.library_path()) == os.path.dirname(
         os.path.abspath(_native.__file__))
     assert isinstance(lib, ctypes.CDLL)
+
+
+def test_tc_operand_kind_switch(lib):
+    """The operand switch needs no device: it returns the previous kind and
+    rejects unknown kinds without changing the setting."""
+    from gstools_gb300 import _native
+
+    assert lib.gst_grid_tc_set_operands(7) == -1
+    prev = _native.set_tc_operands("tf32")
+    assert prev == "f16"
+    assert _native.set_tc_operands("f16") == "tf32"
+    with pytest.raises(ValueError):
+        _native.set_tc_operands("bf16")

@@ -279,3 +279,52 @@ def test_tc_host_entry_points(cuda_lib, kind, shape, out_dtype):
         got, norm = host[idx], np.sqrt(np.sum(fac ** 2))
     d = (got.astype(np.float64) - ref) / norm
     assert np.sqrt(np.mean(d ** 2)) <= RMS_SIGMA and np.abs(d).max() <= MAX_SIGMA
+
+
+@pytest.fixture
+def tf32_operands(cuda_lib):
+    from gstools_gb300 import _native
+
+    prev = _native.set_tc_operands("tf32")
+    yield
+    _native.set_tc_operands(prev)
+
+
+@pytest.mark.parametrize("dim,shape,n_modes", [
+    (2, (300, 257), 203), (3, (40, 33, 70), 500)])
+def test_tc_tf32_operands(tf32_operands, dim, shape, n_modes):
+    """The 3xTF32 operand variant keeps the same bar as the default FP16 one."""
+    cov, z1, z2 = case(dim * 31 + n_modes, dim, n_modes)
+    axes = [np.arange(float(n)) * 0.7 for n in shape]
+    ref = grid_ref(cov, z1, z2, axes)
+    got = gg.summate_grid(cov, z1, z2, axes, precision="mixed",
+                          method="tensor")
+    rms, mx = errors(got, ref, n_modes)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (rms, mx)
+
+
+@pytest.mark.parametrize("amp", [1e-7, 3e-3, 1.0, 5e4, 1e9])
+def test_tc_amplitude_range(cuda_lib, amp):
+    """FP16 operands: amplitudes far outside FP16 range are normalised by a
+    power of two, so the relative error does not depend on their size."""
+    cov, z1, z2 = case(17, 3, 300)
+    axes = [np.arange(24.0), np.arange(17.0) * 1.3, np.arange(40.0) * 0.6]
+    ref = grid_ref(cov, z1, z2, axes)
+    got = gg.summate_grid(cov, amp * z1, amp * z2, axes, precision="mixed",
+                          method="tensor")
+    rms, mx = errors(got / amp, ref, 300)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (rms, mx)
+
+
+def test_tc_fourier_small_spectrum_factor(cuda_lib):
+    """summate_fourier with spectrum factors spanning 8 decades (the decay of
+    a spectral density) keeps the bar relative to the field's scale."""
+    cov, z1, z2 = case(23, 2, 400)
+    fac = np.exp(-np.linspace(0.0, 18.0, 400)) * 1e-3
+    shape = (60, 70)
+    axes = [np.linspace(-10.0, 30.0, n) for n in shape]
+    grid = np.array(np.meshgrid(*axes, indexing="ij")).reshape(2, -1)
+    ref = oracle.c_summate_fourier(fac, cov, z1, z2, grid).reshape(shape)
+    got = gg.summate_fourier_grid(fac, cov, z1, z2, axes)
+    d = (got - ref) / np.sqrt(np.sum(fac ** 2))
+    assert np.sqrt(np.mean(d ** 2)) <= RMS_SIGMA and np.abs(d).max() <= MAX_SIGMA
