@@ -271,28 +271,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// 32 lanes x 32 consecutive FP32 columns of tensor memory.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, "
-        "%29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]),
-          "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
-          "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-          "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr)
-        : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // ------------------------------------------------------------------ tables --
 
 struct GridGeom {
@@ -971,29 +949,30 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
-// Zeroes the output of the split pair tiles (their parts add into it).
+// Zeroes the output of the split pair tiles (their parts add into it): one
+// warp per (tile, row), 32 consecutive z values per store instruction.
 __global__ void zero_split_tiles_kernel(GridGeom g, GridArgs a, int64_t first_tile,
                                         int64_t n_tiles, int tx, int ty) {
     const int64_t rows = 2 * static_cast<int64_t>(tx) * ty;
-    const int64_t total = n_tiles * rows * kTileCols;
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-         i < total; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t zl = i % kTileCols;
-        const int64_t r = (i / kTileCols) % rows;
-        const int64_t pair = a.tile_offset + first_tile + i / (kTileCols * rows);
-        const int64_t zb = pair % a.pair_blocks[2];
-        const int64_t yb = (pair / a.pair_blocks[2]) % a.pair_blocks[1];
-        const int64_t xb = pair / (a.pair_blocks[2] * a.pair_blocks[1]);
-        const int64_t x = xb * 2 * tx + r / ty;
-        const int64_t y = yb * ty + r % ty;
-        const int64_t z = zb * kTileCols + zl;
-        if (x < g.n[0] && y < g.n[1] && z < g.n[2]) {
-            const int64_t o = (x * g.n[1] + y) * g.n[2] + z;
-            if (a.out_f32)
-                static_cast<float *>(a.out)[o] = 0.0f;
-            else
-                static_cast<double *>(a.out)[o] = 0.0;
-        }
+    const int64_t warp_id = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp_id >= n_tiles * rows) return;
+    const int64_t r = warp_id % rows;
+    const int64_t pair = a.tile_offset + first_tile + warp_id / rows;
+    const int64_t zb = pair % a.pair_blocks[2];
+    const int64_t yb = (pair / a.pair_blocks[2]) % a.pair_blocks[1];
+    const int64_t xb = pair / (a.pair_blocks[2] * a.pair_blocks[1]);
+    const int64_t x = xb * 2 * tx + r / ty;
+    const int64_t y = yb * ty + r % ty;
+    if (x >= g.n[0] || y >= g.n[1]) return;
+    const int64_t z0 = zb * kTileCols;
+    const int64_t nz = min(static_cast<int64_t>(kTileCols), g.n[2] - z0);
+    const int64_t o = (x * g.n[1] + y) * g.n[2] + z0;
+    for (int64_t z = lane; z < nz; z += 32) {
+        if (a.out_f32)
+            static_cast<float *>(a.out)[o + z] = 0.0f;
+        else
+            static_cast<double *>(a.out)[o + z] = 0.0;
     }
 }
 
@@ -1159,9 +1138,8 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
     args.stages_per_part = ceil_div(p.g.n_stages, split);
     if (split > 1) {
         const int tx = p.g.tile[0], ty = p.g.tile[1];
-        const int64_t work = tail * 2 * tx * ty * kTileCols;
-        const int blocks = static_cast<int>(std::min<int64_t>(ceil_div(work, 256),
-                                                              sm_count() * 8));
+        const int64_t warps = tail * 2 * tx * ty;   // one per (tile, row)
+        const int blocks = static_cast<int>(ceil_div(warps * 32, 256));
         zero_split_tiles_kernel<<<blocks, 256, 0, s>>>(p.g, args, args.n_full, tail,
                                                        tx, ty);
         GST_TRY_CUDA(cudaGetLastError());
