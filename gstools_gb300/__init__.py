@@ -19,7 +19,7 @@ a C ABI, include/gstools_gb300.h); there is no CPU fallback.
 from . import config
 from .batched import BatchedSummator
 from .covmodel import CovModel, Exponential, Gaussian, Matern
-from .generator import IncomprRandMeth, RandMeth
+from .generator import Fourier, IncomprRandMeth, RandMeth
 from .hook import install, uninstall
 from .rng import RNG, MasterRNG
 from .srf import SRF
@@ -37,6 +37,7 @@ __version__ = "0.1.0"
 __all__ = [
     "config",
     "BatchedSummator",
+    "Fourier",
     "CovModel",
     "Gaussian",
     "Exponential",

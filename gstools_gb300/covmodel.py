@@ -206,6 +206,10 @@ class CovModel:
     def spectral_density(self, k):  # pragma: no cover - abstract
         raise NotImplementedError
 
+    def spectrum(self, k):
+        """Spectrum ``var * spectral_density(k)`` (covmodel/base.py:511-533)."""
+        return self.spectral_density(k) * self.var
+
     def spectral_rad_pdf(self, r):
         """Radial spectral pdf (covmodel/tools.py:374-405)."""
         r = np.asarray(np.abs(r), dtype=np.double)

@@ -4,7 +4,7 @@ A reduced mirror of the reference's ``SRF`` (src/gstools/field/srf.py:25-186)
 and of the position handling of ``Field.pre_pos`` / ``post_field``
 (src/gstools/field/base.py:254-349), covering what the summation path needs:
 generator selection by name ("RandMeth", "IncomprRandMeth", "VectorField",
-"VelocityField") or class, ``update(model, seed)``, isometrized unstructured
+"VelocityField", "Fourier") or class, ``update(model, seed)``, isometrized unstructured
 positions, structured grids and a constant (scalar or per-component) mean.
 Normalizers, trends, upscaling and plotting are not part of this package.
 
@@ -14,7 +14,7 @@ Structured grids never materialise the meshgrid: the generator's
 
 import numpy as np
 
-from .generator import IncomprRandMeth, RandMeth
+from .generator import Fourier, IncomprRandMeth, RandMeth
 
 __all__ = ["SRF", "GENERATOR"]
 
@@ -23,6 +23,7 @@ GENERATOR = {
     "IncomprRandMeth": IncomprRandMeth,
     "VectorField": IncomprRandMeth,
     "VelocityField": IncomprRandMeth,
+    "Fourier": Fourier,
 }
 
 
@@ -37,7 +38,7 @@ class SRF:
         self.pos = None
         self.mesh_type = None
         gen = GENERATOR[generator] if generator in GENERATOR else generator
-        if not (isinstance(gen, type) and issubclass(gen, RandMeth)):
+        if not (isinstance(gen, type) and issubclass(gen, (RandMeth, Fourier))):
             raise ValueError(f"SRF: unknown or wrong generator: {generator}")
         self.generator = gen(model, **generator_kwargs)
         self.value_type = self.generator.value_type

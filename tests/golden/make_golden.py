@@ -14,6 +14,7 @@ assert on this path is reproduced here (``assertAlmostEqual``'s 7 places):
 * tests/test_incomprrandmeth.py:36-38, 58-59
 * tests/test_srf.py:269-275
 * tests/test_rng.py:22-37
+* tests/test_fouriergen.py:47-57 (Fourier generator through SRF)
 
 The 3-D RandMeth goldens (test_randmeth.py:45-46, 65-66;
 test_incomprrandmeth.py:42-44) need emcee's MCMC sampler, which is absent, so
@@ -153,6 +154,39 @@ def reference_goldens(gs):
     out["srf_incompr_struct/expected"] = np.array([1.07812013, 1.06180674])
     out["srf_incompr_struct/index"] = np.array([[0, 0, 0], [0, 1, 0]])
     out["srf_incompr_struct/field"] = fld
+
+    # tests/test_fouriergen.py:14-57: Fourier generator through SRF,
+    # structured 1-D / 2-D / 3-D Gaussian fields
+    f_seed = 19900408
+    f_models = [gs.Gaussian(dim=1, var=0.5, len_scale=10.0),
+                gs.Gaussian(dim=2, var=2.0, len_scale=30.0),
+                gs.Gaussian(dim=3, var=2.1, len_scale=21.0)]
+    f_period = [80, 30, 91]
+    f_axes = [np.linspace(0, f_period[0], 11), np.linspace(0, f_period[1], 31),
+              np.linspace(0, f_period[2], 13)]
+    f_modes = [12, 6, 14]
+    f_expected = [0.6236929351309081, -0.1431996611581266, -1.0433325279452803]
+    for d in (1, 2, 3):
+        srf = gs.SRF(f_models[d - 1], generator="Fourier", mode_no=f_modes[:d],
+                     period=f_period[:d], seed=f_seed)
+        fld = srf(tuple(f_axes[:d]), mesh_type="structured")
+        check(fld[(0,) * d], f_expected[d - 1], f"fourier_{d}d{(0,) * d}")
+        gen = srf.generator
+        name = f"fourier_{d}d"
+        out[f"{name}/modes"] = np.array(gen.modes, dtype=np.float64)
+        out[f"{name}/z1"] = np.array(gen._z_1, dtype=np.float64)
+        out[f"{name}/z2"] = np.array(gen._z_2, dtype=np.float64)
+        out[f"{name}/spectrum_factor"] = np.array(gen._spectrum_factor,
+                                                  dtype=np.float64)
+        out[f"{name}/period"] = np.array(f_period[:d], dtype=np.float64)
+        out[f"{name}/mode_no"] = np.array(f_modes[:d], dtype=np.int64)
+        out[f"{name}/var"] = np.float64(f_models[d - 1].var)
+        out[f"{name}/len_scale"] = np.float64(f_models[d - 1].len_scale)
+        out[f"{name}/seed"] = np.int64(f_seed)
+        for i in range(d):
+            out[f"{name}/axis{i}"] = f_axes[i]
+        out[f"{name}/field"] = np.asarray(fld)
+        out[f"{name}/expected"] = np.float64(f_expected[d - 1])
 
     # tests/test_rng.py:20-37: normal streams of RNG(19031977)
     rng = RNG(seed)
