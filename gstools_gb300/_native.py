@@ -24,6 +24,9 @@ GST_OUT_F64 = 0
 GST_OUT_F32 = 1
 GST_TC_TF32 = 0
 GST_TC_F16 = 1
+GST_MODEL_GAUSSIAN = 0
+GST_MODEL_EXPONENTIAL = 1
+GST_MODEL_MATERN = 2
 
 _c_int = ctypes.c_int
 _i64 = ctypes.c_int64
@@ -96,6 +99,10 @@ SIGNATURES = {
                                                   _ptr, _ptr, _ptr, _ptr, _c_int,
                                                   _dbl, _ptr]),
     "gst_grid_tc_set_operands": (_c_int, [_c_int]),
+    "gst_batch_sample_modes": (_c_int, [_c_int, _i64, _i64, _ptr, _c_int, _dbl,
+                                        _ptr, _ptr, _ptr, _ptr, _ptr, _ptr]),
+    "gst_philox4x64_fill": (_c_int, [ctypes.c_uint64, ctypes.c_uint64, _i64,
+                                     ctypes.c_uint64, _ptr, _ptr]),
     "gst_peak_probe": (_c_int, [_c_int, _i64, _ptr, ctypes.POINTER(_dbl),
                                 _ptr]),
 }

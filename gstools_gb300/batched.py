@@ -12,6 +12,13 @@ graph.
 The tile shape is chosen per ensemble shape by timing the kernel variants on
 the loaded data (:meth:`BatchedSummator.tune`); the choice is cached per shape
 for the process.
+
+The modes can also be drawn on the device (:meth:`BatchedSummator.sample`):
+all realizations' amplitudes, directions and radii in one launch from a
+counter-based Philox stream per realization seed, instead of the reference's
+host loop over ``RandMeth.reset_seed`` (src/gstools/field/generator.py:
+346-387).  That stream is not the reference's MT19937 stream; the
+distributions are the models' spectral laws.
 """
 
 import ctypes
@@ -92,6 +99,66 @@ class BatchedSummator:
                                            + self.points.tobytes()).hexdigest())
 
     # -- data -------------------------------------------------------------
+    def load_points(self, pos):
+        """Copy the per-realization point sets (already isometrized, the
+        reference's (dim, n) layout) into the device buffer."""
+        if len(pos) != self.n_items:
+            raise ValueError("one point set per realization expected")
+        xx = np.zeros((self.dim, self.total_points))
+        for r in range(self.n_items):
+            p0, p1 = self.point_off[r], self.point_off[r + 1]
+            x = np.asarray(pos[r], dtype=np.float64).reshape(self.dim, -1)
+            if x.shape[1] != p1 - p0:
+                raise ValueError(f"realization {r}: sizes do not match the plan")
+            xx[:, p0:p1] = x
+        self.pos.copy_(torch.from_numpy(xx).pin_memory(), non_blocking=True)
+
+    def sample(self, model, seeds, len_scales=None, variances=None):
+        """Draw every realization's modes on the device (asynchronous).
+
+        ``model`` (Gaussian, Exponential or Matern with nu <= 20) gives the
+        spectral law; ``seeds`` one uint64 per realization; ``len_scales``
+        and ``variances`` override the model's per realization.  Sets the
+        scales to ``sqrt(var_r / N_r)`` (RandMeth's normalisation).
+        """
+        kinds = {"Gaussian": _native.GST_MODEL_GAUSSIAN,
+                 "Exponential": _native.GST_MODEL_EXPONENTIAL,
+                 "Matern": _native.GST_MODEL_MATERN}
+        name = type(model).__name__
+        if name not in kinds:
+            raise ValueError(f"device sampling supports {sorted(kinds)}, "
+                             f"not {name}")
+        if model.dim != self.dim:
+            raise ValueError("model dimension does not match the plan")
+        nu = float(getattr(model, "nu", 0.0)) if name == "Matern" else 0.0
+        if name == "Matern" and not 0.0 < nu <= 20.0:
+            raise ValueError("device sampling of Matern needs 0 < nu <= 20")
+        seeds = np.array(seeds, dtype=np.uint64).reshape(-1)
+        if seeds.size != self.n_items:
+            raise ValueError("one seed per realization expected")
+        ls = (np.full(self.n_items, model.len_scale) if len_scales is None
+              else np.asarray(len_scales, dtype=np.float64).reshape(-1))
+        var = (np.full(self.n_items, model.var) if variances is None
+               else np.asarray(variances, dtype=np.float64).reshape(-1))
+        if ls.size != self.n_items or var.size != self.n_items:
+            raise ValueError("one len_scale / variance per realization expected")
+        if getattr(self, "_mode_off_dev", None) is None:
+            self._mode_off_dev = torch.from_numpy(
+                self.mode_off.astype(np.int64)).to(self.dev)
+        params = np.concatenate((seeds.view(np.float64), ls / model.rescale))
+        self._sample_params = torch.from_numpy(params).to(self.dev)
+        off = self._mode_off_dev
+        sd = self._sample_params[: self.n_items]
+        lsr = self._sample_params[self.n_items:]
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+        _native.call("gst_batch_sample_modes", self.dim, self.n_items,
+                     self.total_modes, _ptr(off), kinds[name], nu, _ptr(sd),
+                     _ptr(lsr), _ptr(self.cov), _ptr(self.z1), _ptr(self.z2),
+                     stream)
+        counts = np.maximum(self.modes, 1)
+        self.scales[: self.n_items].copy_(
+            torch.from_numpy(np.sqrt(var / counts)))
+
     def load(self, cov_samples, z_1, z_2, pos, scales=None):
         """Copy one ensemble's inputs (lists of per-realization arrays, the
         reference's layouts) into the device buffers."""

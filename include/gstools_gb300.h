@@ -295,6 +295,37 @@ int gst_batch_run(int dim, int64_t n_items, const int64_t *mode_counts,
                   const double *scales, void *out, int out_type,
                   void *workspace, size_t workspace_bytes, void *stream);
 
+/* ----------------------------------------------------------------------- */
+/* Device-side spectral sampling for ensembles (replaces the per-realization */
+/* host loop of RandMeth.reset_seed, src/gstools/field/generator.py:346-387, */
+/* with the RNG of src/gstools/random/rng.py:38-203).  Draws, for every      */
+/* realization r of a batch laid out as gst_batch_run expects, its          */
+/* mode_counts[r] modes: z_1, z_2 ~ N(0, 1), directions uniform on the unit  */
+/* sphere and radii from the model's radial spectral law with length scale  */
+/* len_rescaled[r]: Gaussian (normal), Exponential (multivariate t, 1 dof), */
+/* Matern nu (multivariate t, 2 nu dof; 0 < nu <= 20).  Mode j of           */
+/* realization r is a pure function of (seeds[r], j) through a Philox4x64-10 */
+/* stream (key (seeds[r], 0), counter (j, block, 0, 0)), so the draw is      */
+/* reproducible and independent of the batch it is part of.  It is not the  */
+/* reference's MT19937 stream.  mode_offsets (device, n_items + 1) are the  */
+/* prefix sums of the mode counts, seeds (device, uint64) and len_rescaled  */
+/* (device) one per realization; cov (dim, total_modes), z_1, z_2 device   */
+/* outputs.  Asynchronous, allocates nothing, may be captured in a graph.   */
+/* No counterpart in the reference (its sampling is host-side).             */
+/* ----------------------------------------------------------------------- */
+#define GST_MODEL_GAUSSIAN 0
+#define GST_MODEL_EXPONENTIAL 1
+#define GST_MODEL_MATERN 2
+int gst_batch_sample_modes(int dim, int64_t n_items, int64_t total_modes,
+                           const int64_t *mode_offsets, int model, double nu,
+                           const uint64_t *seeds, const double *len_rescaled,
+                           double *cov, double *z_1, double *z_2, void *stream);
+/* The raw Philox4x64-10 stream: out[4 i .. 4 i + 3] = Philox(counter       */
+/* (i, counter1, 0, 0), key (key0, key1)) for i < n_blocks (device out).    */
+/* For checking the generator against known-answer vectors.                 */
+int gst_philox4x64_fill(uint64_t key0, uint64_t key1, int64_t n_blocks,
+                        uint64_t counter1, uint64_t *out, void *stream);
+
 /* Operand format of the tensor-core grid path's split GEMM (hi*hi + hi*lo +
  * lo*hi): GST_TC_F16 (default; FP16 products at twice the TF32 rate, the
  * amplitudes normalised by a power of two) or GST_TC_TF32.  Both keep 10

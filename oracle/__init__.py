@@ -13,11 +13,17 @@ Two independent restatements of the reference formulas
   library built from ``summate_oracle.c`` (the primary oracle and the timed CPU
   baseline);
 * ``np_summate`` / ``np_summate_incompr`` / ``np_summate_fourier``: a chunked
-  numpy witness used to cross-check the C oracle.
+  numpy witness used to cross-check the C oracle;
+* ``c_sample_modes`` / ``c_philox4x64``: the C restatement of the device
+  spectral sampler (``sample_oracle.c``), its Philox stream pinned to numpy's
+  Philox bit generator by the tests.
 """
 
 from .oracle import (  # noqa: F401
+    MODEL_KINDS,
     build,
+    c_philox4x64,
+    c_sample_modes,
     c_summate,
     c_summate_fourier,
     c_summate_incompr,

@@ -5,6 +5,10 @@ Every function here restates the reference's formulas:
 * summate          -- src/gstools/field/generator.py:193-199
 * summate_incompr  -- src/gstools/field/generator.py:479-495
 * summate_fourier  -- src/gstools/field/generator.py:682-689
+* sample_modes     -- the device spectral sampler of
+                      gstools_gb300/csrc/gst_sampling.cu (Philox4x64-10
+                      stream, sphere formulas of src/gstools/random/rng.py:
+                      142-193, the models' analytic radial laws)
 
 Inputs follow the reference's array layouts: ``cov_samples`` (dim, N),
 ``z_1``/``z_2`` (N,), ``pos`` (dim, n), all float64.
@@ -30,12 +34,12 @@ def library_path():
 
 def build(force=False):
     """Compile the C oracle with its Makefile (gcc, OpenMP)."""
-    src = os.path.join(_HERE, "summate_oracle.c")
+    srcs = [os.path.join(_HERE, f) for f in ("summate_oracle.c", "sample_oracle.c")]
     out = library_path()
     if (
         not force
         and os.path.exists(out)
-        and os.path.getmtime(out) >= os.path.getmtime(src)
+        and os.path.getmtime(out) >= max(os.path.getmtime(f) for f in srcs)
     ):
         return out
     subprocess.run(["make", "-s", "-C", _HERE, "-B"], check=True)
@@ -61,6 +65,13 @@ def _load():
                            ctypes.c_int]
             lib.oracle_num_threads.restype = ctypes.c_int
             lib.oracle_num_threads.argtypes = []
+            u64 = ctypes.c_uint64
+            lib.oracle_philox4x64.restype = None
+            lib.oracle_philox4x64.argtypes = [u64] * 6 + [ctypes.POINTER(u64)]
+            lib.oracle_sample_modes.restype = ctypes.c_int
+            lib.oracle_sample_modes.argtypes = [
+                ctypes.c_int, i64, i64, ctypes.POINTER(i64), ctypes.c_int,
+                ctypes.c_double, ctypes.POINTER(u64), dp, dp, dp, dp]
             _lib = lib
     return _lib
 
@@ -175,3 +186,35 @@ def np_summate_fourier(spectrum_factor, modes, z_1, z_2, pos, chunk=4096):
             phase
         )
     return out
+
+
+MODEL_KINDS = {"Gaussian": 0, "Exponential": 1, "Matern": 2}
+
+
+def c_philox4x64(counter, key):
+    """Philox4x64-10 of one 256-bit counter under a 128-bit key."""
+    out = (ctypes.c_uint64 * 4)()
+    _load().oracle_philox4x64(*[int(c) for c in counter], *[int(k) for k in key],
+                              out)
+    return np.array(list(out), dtype=np.uint64)
+
+
+def c_sample_modes(dim, mode_counts, model, nu, seeds, len_rescaled):
+    """CPU restatement of gst_batch_sample_modes: (cov (dim, M), z1, z2)."""
+    counts = np.ascontiguousarray(mode_counts, dtype=np.int64)
+    off = np.ascontiguousarray(np.concatenate(([0], np.cumsum(counts))),
+                               dtype=np.int64)
+    total = int(off[-1])
+    seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+    ls = _f64(len_rescaled)
+    cov = np.zeros((dim, total))
+    z1 = np.zeros(total)
+    z2 = np.zeros(total)
+    rc = _load().oracle_sample_modes(
+        dim, len(counts), total, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+        MODEL_KINDS[model] if isinstance(model, str) else int(model), float(nu),
+        seeds.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _ptr(ls),
+        _ptr(cov), _ptr(z1), _ptr(z2))
+    if rc:
+        raise ValueError(f"oracle_sample_modes failed with code {rc}")
+    return cov, z1, z2
