@@ -68,7 +68,8 @@ def parse():
     p.add_argument("--operands", default="f16", choices=["f16", "tf32"],
                    help="operand format of the tensor-core split GEMM")
     p.add_argument("--workload", default="grid",
-                   choices=["grid", "points", "ensemble", "incompr", "adjoint"],
+                   choices=["grid", "points", "ensemble", "incompr", "adjoint",
+                            "krige"],
                    help="grid: the headline (3-D Exponential, 256^3, 2000 "
                         "modes); the others are the remaining BASELINE "
                         "configurations")
@@ -547,6 +548,85 @@ def _line(args, workload, value, t_step, dtype, config, **extra):
     return line
 
 
+def wl_krige(args, torch, gg, flush):
+    """Ordinary kriging with an exponential covariance (var 1, length scale
+    50): 1000 conditioning points and 65 536 target points uniform in
+    [0, 500]^2; the kernels' inputs built the reference's way
+    (src/gstools/krige/base.py:330-405): M = inverse of the bordered
+    covariance matrix, V = covariances to the targets plus the unbiasedness
+    row.  Work unit: the 2 (K+1)^2 n flops of the nested sums."""
+    import oracle
+    from scipy.spatial.distance import cdist
+
+    rng = np.random.RandomState(20170519)
+    n_cond, n_pts = 1000, 65536
+    cpos = rng.uniform(0.0, 500.0, (2, n_cond))
+    tpos = rng.uniform(0.0, 500.0, (2, n_pts))
+    cond = np.append(rng.normal(size=n_cond), 0.0)
+    cov = lambda h: np.exp(-h / 50.0)
+    a = np.empty((n_cond + 1, n_cond + 1))
+    a[:n_cond, :n_cond] = cov(cdist(cpos.T, cpos.T))
+    a[n_cond, :n_cond] = a[:n_cond, n_cond] = 1.0
+    a[n_cond, n_cond] = 0.0
+    mat = np.linalg.inv(a)
+    vecs = np.empty((n_cond + 1, n_pts))
+    vecs[:n_cond] = cov(cdist(cpos.T, tpos.T))
+    vecs[n_cond] = 1.0
+    k = n_cond + 1
+    flops = 2.0 * k * k * n_pts
+    dev = torch.device("cuda", torch.cuda.current_device())
+    dm, dv, dc = (torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+                  for x in (mat, vecs, cond))
+    step = lambda: gg.calc_field_krige_and_variance(dm, dv, dc)
+    t = _timed_events(torch, step, args.steps, args.warmup, flush)
+    f, e = step()
+    sample = 512
+    t0 = time.perf_counter()
+    fo, eo = oracle.c_krige(mat, vecs[:, :sample], cond)
+    t_cpu = time.perf_counter() - t0
+    _, _, scale = oracle.np_krige(mat, vecs[:, :sample], cond)
+    err = float(max(np.max(np.abs(f[:sample].cpu().numpy() - fo) / scale),
+                    np.max(np.abs(e[:sample].cpu().numpy() - eo) / scale)))
+    t0 = time.perf_counter()
+    fe = gg.calc_field_krige_and_variance(mat, vecs, cond)
+    te2e = time.perf_counter() - t0
+    peak64 = None
+    try:
+        sink = torch.zeros(256, dtype=torch.float32, device=dev)
+        ops = ctypes.c_double(0.0)
+        from gstools_gb300 import _native
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _native.call("gst_peak_probe", 1, 64, ctypes.c_void_p(sink.data_ptr()),
+                     ctypes.byref(ops), stream)
+        e1.record()
+        e1.synchronize()
+        peak64 = ops.value / (e0.elapsed_time(e1) / 1e3) / 1e12
+    except Exception:  # noqa: BLE001 - the probe is informational here
+        pass
+    achieved = flops / t / 1e12
+    return dict(
+        metric="GFLOP/s of the kriging field + variance (FP64)",
+        value=flops / t / 1e9, unit="GFLOP/s", n_gpus=1, steps=args.steps,
+        warmup=args.warmup, ms_per_step=t * 1e3, higher_is_better=True,
+        scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+        config={"workload": "ordinary_krige_exp2d_cond1000_pts65536",
+                "n_cond": k, "n_pts": n_pts},
+        error_vs_oracle={"max_rel_to_term_scale": err, "points": sample},
+        roofline={"bound": "fp64", "achieved": achieved, "peak": peak64,
+                  "unit": "TFLOP/s",
+                  "frac": achieved / peak64 if peak64 else None,
+                  "kernel": "krige_kernel", "peak_source": "gst_peak_probe FP64 FMA"},
+        cpu_baseline={"value": 2.0 * k * k * sample / t_cpu / 1e9,
+                      "unit": "GFLOP/s", "cores": oracle.num_threads(),
+                      "kind": "port", "sample": f"{sample} target points"},
+        e2e={"value": flops / te2e / 1e9, "unit": "GFLOP/s",
+             "h2d_bytes_per_step": int(mat.nbytes + vecs.nbytes + cond.nbytes),
+             "d2h_bytes_per_step": int(fe[0].nbytes + fe[1].nbytes)},
+        gpu_launches=1)
+
+
 def wl_points(args, torch, gg, flush):
     """2-D Gaussian, var 1, len_scale 10, 1000 modes (reference RNG, seed
     20170519), 100 000 points uniform in [0, 100]^2."""
@@ -839,7 +919,7 @@ def run_workload(args):
     torch.cuda.set_device(0)
     build.build()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    fn = {"points": wl_points, "ensemble": wl_ensemble,
+    fn = {"points": wl_points, "ensemble": wl_ensemble, "krige": wl_krige,
           "incompr": wl_incompr, "adjoint": wl_adjoint}[args.workload]
     clocks = Clocks(0)
     clocks.start()

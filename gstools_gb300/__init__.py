@@ -21,6 +21,7 @@ from .batched import BatchedSummator
 from .covmodel import CovModel, Exponential, Gaussian, Matern
 from .generator import Fourier, IncomprRandMeth, RandMeth
 from .hook import install, uninstall
+from .krige import calc_field_krige, calc_field_krige_and_variance
 from .rng import RNG, MasterRNG
 from .srf import SRF
 from .summator import (
@@ -38,6 +39,8 @@ __all__ = [
     "config",
     "BatchedSummator",
     "Fourier",
+    "calc_field_krige",
+    "calc_field_krige_and_variance",
     "CovModel",
     "Gaussian",
     "Exponential",

@@ -101,6 +101,8 @@ SIGNATURES = {
     "gst_grid_tc_set_operands": (_c_int, [_c_int]),
     "gst_batch_sample_modes": (_c_int, [_c_int, _i64, _i64, _ptr, _c_int, _dbl,
                                         _ptr, _ptr, _ptr, _ptr, _ptr, _ptr]),
+    "gst_calc_field_krige": (_c_int, [_i64, _i64, _ptr, _ptr, _ptr, _ptr, _ptr,
+                                      _ptr]),
     "gst_philox4x64_fill": (_c_int, [ctypes.c_uint64, ctypes.c_uint64, _i64,
                                      ctypes.c_uint64, _ptr, _ptr]),
     "gst_peak_probe": (_c_int, [_c_int, _i64, _ptr, ctypes.POINTER(_dbl),

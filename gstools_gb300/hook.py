@@ -6,17 +6,23 @@ The reference resolves its summators per call through module globals:
 (:554-560) and ``Fourier.__call__`` calls ``_summate_fourier(...)``
 (:682-689).  Rebinding those three names routes every ``SRF`` / ``CondSRF`` /
 generator call of that process through this package, with no other change
-to the reference.
+to the reference.  Kriging is routed the same way: ``Krige._summate``
+(src/gstools/krige/base.py:307-320) calls the module globals
+``_calc_field_krige`` / ``_calc_field_krige_and_variance`` (:42-60), which
+:func:`install` rebinds in ``gstools.krige.base`` when that module is
+importable.
 """
 
 import sys
 
 from . import config
+from .krige import calc_field_krige, calc_field_krige_and_variance
 from .summator import summate, summate_fourier, summate_incompr
 
 _saved = {}
 
 _NAMES = ("_summate", "_summate_incompr", "_summate_fourier")
+_KRIGE_NAMES = ("_calc_field_krige", "_calc_field_krige_and_variance")
 
 
 def _generator_module(module=None):
@@ -28,12 +34,26 @@ def _generator_module(module=None):
     return mod
 
 
-def install(module=None, precision=None):
-    """Route the reference's summation calls to the GPU kernels.
+def _krige_module(module=None):
+    if module is not None:
+        return module
+    mod = sys.modules.get("gstools.krige.base")
+    if mod is None:
+        try:
+            import gstools.krige.base as mod  # noqa: F811
+        except ImportError:
+            return None
+    return mod
 
-    ``module`` defaults to ``gstools.field.generator``; ``precision``
-    ("f64" or "mixed") is fixed for the installed wrappers (``None`` follows
-    ``gstools_gb300.config.PRECISION`` at call time).  Returns the module.
+
+def install(module=None, precision=None, krige_module=None):
+    """Route the reference's summation and kriging calls to the GPU kernels.
+
+    ``module`` defaults to ``gstools.field.generator`` and ``krige_module``
+    to ``gstools.krige.base`` (skipped when it cannot be imported);
+    ``precision`` ("f64" or "mixed") is fixed for the installed summators
+    (``None`` follows ``gstools_gb300.config.PRECISION`` at call time).
+    Kriging always runs in FP64.  Returns the generator module.
     """
     mod = _generator_module(module)
     if precision is not None:
@@ -57,14 +77,33 @@ def install(module=None, precision=None):
     mod._summate = _summate
     mod._summate_incompr = _summate_incompr
     mod._summate_fourier = _summate_fourier
+
+    kmod = _krige_module(krige_module)
+    if kmod is not None:
+        if id(kmod) not in _saved:
+            _saved[id(kmod)] = {n: getattr(kmod, n) for n in _KRIGE_NAMES}
+
+        def _calc_field_krige(krig_mat, krig_vecs, cond, num_threads=None):
+            return calc_field_krige(krig_mat, krig_vecs, cond, num_threads)
+
+        def _calc_field_krige_and_variance(krig_mat, krig_vecs, cond,
+                                           num_threads=None):
+            return calc_field_krige_and_variance(krig_mat, krig_vecs, cond,
+                                                 num_threads)
+
+        kmod._calc_field_krige = _calc_field_krige
+        kmod._calc_field_krige_and_variance = _calc_field_krige_and_variance
     return mod
 
 
-def uninstall(module=None):
-    """Restore the summators that :func:`install` replaced."""
+def uninstall(module=None, krige_module=None):
+    """Restore the functions that :func:`install` replaced."""
     mod = _generator_module(module)
-    saved = _saved.pop(id(mod), None)
-    if saved:
-        for name, fct in saved.items():
-            setattr(mod, name, fct)
+    for m in (mod, _krige_module(krige_module)):
+        if m is None:
+            continue
+        saved = _saved.pop(id(m), None)
+        if saved:
+            for name, fct in saved.items():
+                setattr(m, name, fct)
     return mod

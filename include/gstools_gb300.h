@@ -326,6 +326,22 @@ int gst_batch_sample_modes(int dim, int64_t n_items, int64_t total_modes,
 int gst_philox4x64_fill(uint64_t key0, uint64_t key1, int64_t n_blocks,
                         uint64_t counter1, uint64_t *out, void *stream);
 
+/* ----------------------------------------------------------------------- */
+/* Kriging field and error variance (CondSRF / Krige hot loop).  Replaces   */
+/* gstools_cython.krige.calc_field_krige and                                */
+/* calc_field_krige_and_variance (imported src/gstools/krige/base.py:16-19, */
+/* called through _calc_field_krige(_and_variance) at :42-60 from           */
+/* Krige._summate, :307-320).  For the inverted kriging matrix krig_mat      */
+/* (n_cond x n_cond, row-major), the right-hand sides krig_vecs (n_cond x   */
+/* n_pts, row-major) and the condition values cond (n_cond):                */
+/*   field[k] = sum_i cond[i] (M v_k)_i,  error[k] = sum_i v_ik (M v_k)_i    */
+/* (error may be NULL for the field only).  Device pointers; FP64;          */
+/* deterministic.                                                           */
+/* ----------------------------------------------------------------------- */
+int gst_calc_field_krige(int64_t n_cond, int64_t n_pts, const double *krig_mat,
+                         const double *krig_vecs, const double *cond, double *field,
+                         double *error, void *stream);
+
 /* Operand format of the tensor-core grid path's split GEMM (hi*hi + hi*lo +
  * lo*hi): GST_TC_F16 (default; FP16 products at twice the TF32 rate, the
  * amplitudes normalised by a power of two) or GST_TC_TF32.  Both keep 10

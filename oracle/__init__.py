@@ -14,6 +14,8 @@ Two independent restatements of the reference formulas
   baseline);
 * ``np_summate`` / ``np_summate_incompr`` / ``np_summate_fourier``: a chunked
   numpy witness used to cross-check the C oracle;
+* ``c_krige`` / ``np_krige``: the kriging kernels of gstools-cython
+  (``krige_oracle.c``) and a numpy witness;
 * ``c_sample_modes`` / ``c_philox4x64``: the C restatement of the device
   spectral sampler (``sample_oracle.c``), its Philox stream pinned to numpy's
   Philox bit generator by the tests.
@@ -22,6 +24,7 @@ Two independent restatements of the reference formulas
 from .oracle import (  # noqa: F401
     MODEL_KINDS,
     build,
+    c_krige,
     c_philox4x64,
     c_sample_modes,
     c_summate,
@@ -29,6 +32,7 @@ from .oracle import (  # noqa: F401
     c_summate_incompr,
     library_path,
     num_threads,
+    np_krige,
     np_summate,
     np_summate_fourier,
     np_summate_incompr,

@@ -5,6 +5,8 @@ Every function here restates the reference's formulas:
 * summate          -- src/gstools/field/generator.py:193-199
 * summate_incompr  -- src/gstools/field/generator.py:479-495
 * summate_fourier  -- src/gstools/field/generator.py:682-689
+* krige            -- calc_field_krige(_and_variance) of gstools-cython, called
+                      by src/gstools/krige/base.py:42-60, 307-320
 * sample_modes     -- the device spectral sampler of
                       gstools_gb300/csrc/gst_sampling.cu (Philox4x64-10
                       stream, sphere formulas of src/gstools/random/rng.py:
@@ -34,7 +36,8 @@ def library_path():
 
 def build(force=False):
     """Compile the C oracle with its Makefile (gcc, OpenMP)."""
-    srcs = [os.path.join(_HERE, f) for f in ("summate_oracle.c", "sample_oracle.c")]
+    srcs = [os.path.join(_HERE, f)
+            for f in ("summate_oracle.c", "sample_oracle.c", "krige_oracle.c")]
     out = library_path()
     if (
         not force
@@ -68,6 +71,8 @@ def _load():
             u64 = ctypes.c_uint64
             lib.oracle_philox4x64.restype = None
             lib.oracle_philox4x64.argtypes = [u64] * 6 + [ctypes.POINTER(u64)]
+            lib.oracle_krige.restype = ctypes.c_int
+            lib.oracle_krige.argtypes = [i64, i64, dp, dp, dp, dp, dp]
             lib.oracle_sample_modes.restype = ctypes.c_int
             lib.oracle_sample_modes.argtypes = [
                 ctypes.c_int, i64, i64, ctypes.POINTER(i64), ctypes.c_int,
@@ -218,3 +223,35 @@ def c_sample_modes(dim, mode_counts, model, nu, seeds, len_rescaled):
     if rc:
         raise ValueError(f"oracle_sample_modes failed with code {rc}")
     return cov, z1, z2
+
+
+def c_krige(krig_mat, krig_vecs, cond, with_error=True):
+    """C restatement of gstools-cython's calc_field_krige(_and_variance):
+    (field, error) or field for M (K, K), V (K, n), cond (K,)."""
+    mat = _f64(np.atleast_2d(krig_mat))
+    vecs = _f64(np.atleast_2d(krig_vecs))
+    cnd = _f64(cond).reshape(-1)
+    k, n = vecs.shape
+    if mat.shape != (k, k) or cnd.size != k:
+        raise ValueError("oracle_krige: M (K, K), V (K, n), cond (K,)")
+    field = np.empty(n)
+    error = np.empty(n) if with_error else None
+    rc = _load().oracle_krige(k, n, _ptr(mat), _ptr(vecs), _ptr(cnd), _ptr(field),
+                              _ptr(error) if with_error else None)
+    if rc:
+        raise ValueError(f"oracle_krige failed with code {rc}")
+    return (field, error) if with_error else field
+
+
+def np_krige(krig_mat, krig_vecs, cond):
+    """numpy witness: (field, error, scale) per target point, with
+    scale = sum_i (|c_i| + |v_i|) (|M| |v|)_i, the magnitude that rounding
+    errors of both nested sums scale with (kriging matrices of smooth
+    covariances are ill-conditioned, so the sums cancel)."""
+    m = np.asarray(krig_mat)
+    v = np.asarray(krig_vecs)
+    mv = m @ v
+    c = np.asarray(cond).reshape(-1, 1)
+    amv = np.abs(m) @ np.abs(v)
+    return ((c * mv).sum(axis=0), (v * mv).sum(axis=0),
+            ((np.abs(c) + np.abs(v)) * amv).sum(axis=0))

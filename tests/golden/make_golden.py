@@ -15,6 +15,9 @@ assert on this path is reproduced here (``assertAlmostEqual``'s 7 places):
 * tests/test_srf.py:269-275
 * tests/test_rng.py:22-37
 * tests/test_fouriergen.py:47-57 (Fourier generator through SRF)
+* tests/test_krige.py:56-153 (kriging: exact at the conditions, structured
+  equals unstructured), with gstools-cython's kriging kernels restated by
+  the C oracle; the arrays each Krige call hands to those kernels are stored
 
 The 3-D RandMeth goldens (test_randmeth.py:45-46, 65-66;
 test_incomprrandmeth.py:42-44) need emcee's MCMC sampler, which is absent, so
@@ -46,8 +49,8 @@ from reference_import import import_gstools  # noqa: E402
 PLACES = 7
 
 
-def check(value, expected, what):
-    if round(abs(value - expected), PLACES) != 0:
+def check(value, expected, what, places=None):
+    if round(abs(value - expected), PLACES if places is None else places) != 0:
         raise AssertionError(f"{what}: got {value!r}, reference {expected!r}")
 
 
@@ -187,6 +190,62 @@ def reference_goldens(gs):
             out[f"{name}/axis{i}"] = f_axes[i]
         out[f"{name}/field"] = np.asarray(fld)
         out[f"{name}/expected"] = np.float64(f_expected[d - 1])
+
+    # tests/test_krige.py:20-153: Simple / Ordinary / Universal kriging of
+    # the test's five conditions; record what Krige hands to the kernels
+    import gstools_cython.krige as ck
+
+    data = np.array([[0.3, 1.2, 0.5, 0.47], [1.9, 0.6, 1.0, 0.56],
+                     [1.1, 3.2, 1.5, 0.74], [3.3, 4.4, 2.0, 1.47],
+                     [4.7, 3.8, 2.5, 1.74]])
+    data_idx = tuple(np.array(data[:, :3] * 10, dtype=int).T)
+    cond_pos = (data[:, 0], data[:, 1], data[:, 2])
+    cond_val = data[:, 3]
+    axes = (np.linspace(0, 5, 51), np.linspace(0, 6, 61), np.linspace(0, 7, 71))
+    recorded = []
+    orig = ck.calc_field_krige_and_variance
+
+    def record(m, v, c, num_threads=None):
+        recorded.append((np.array(m), np.array(v), np.array(c)))
+        return orig(m, v, c)
+
+    ck.calc_field_krige_and_variance = record
+    import gstools.krige.base as kb
+    kb_orig = kb._calc_field_krige_and_variance
+    kb._calc_field_krige_and_variance = lambda m, v, c, num_threads=None: record(m, v, c)
+    try:
+        cases = [
+            ("simple", lambda mdl, d: gs.krige.Simple(mdl, cond_pos[:d], cond_val,
+                                                     np.mean(cond_val)), 2, 2),
+            ("ordinary", lambda mdl, d: gs.krige.Ordinary(mdl, cond_pos[:d],
+                                                          cond_val), 5, 10),
+            ("universal", lambda mdl, d: gs.krige.Universal(mdl, cond_pos[:d],
+                                                            cond_val, "linear"),
+             2, 10),
+        ]
+        for kind, make, var, ls in cases:
+            for Model in (gs.Gaussian, gs.Exponential):
+                for d in (1, 2, 3):
+                    mdl = Model(dim=d, var=var, len_scale=ls, anis=[0.9, 0.8],
+                                angles=[2, 1, 0.5])
+                    krig = make(mdl, d)
+                    recorded.clear()
+                    fld_s, _ = krig.structured(axes[:d])
+                    for i, val in enumerate(cond_val):
+                        check(fld_s[data_idx[:d]][i], val, f"krige_{kind}",
+                              places=2)
+                    name = f"krige_{kind}_{Model.__name__.lower()}_{d}d"
+                    m, v, c = recorded[-1]
+                    v = v[:, :4000]
+                    f, e = oracle.c_krige(m, v, c)
+                    out[f"{name}/mat"] = m
+                    out[f"{name}/vecs"] = v
+                    out[f"{name}/cond"] = c
+                    out[f"{name}/field"] = f
+                    out[f"{name}/error"] = e
+    finally:
+        ck.calc_field_krige_and_variance = orig
+        kb._calc_field_krige_and_variance = kb_orig
 
     # tests/test_rng.py:20-37: normal streams of RNG(19031977)
     rng = RNG(seed)

@@ -54,8 +54,12 @@ def _install_stubs():
                      "unstructured"):
             setattr(vario, name, _unavailable(f"variogram.{name}"))
         krige = types.ModuleType("gstools_cython.krige")
-        for name in ("calc_field_krige", "calc_field_krige_and_variance"):
-            setattr(krige, name, _unavailable(f"krige.{name}"))
+        krige.calc_field_krige = lambda m, v, c, num_threads=None: (
+            oracle.c_krige(m, v, c, with_error=False)
+        )
+        krige.calc_field_krige_and_variance = (
+            lambda m, v, c, num_threads=None: oracle.c_krige(m, v, c)
+        )
         pkg.field, pkg.variogram, pkg.krige = field, vario, krige
         sys.modules.update({
             "gstools_cython": pkg,
