@@ -69,7 +69,7 @@ def parse():
                    help="operand format of the tensor-core split GEMM")
     p.add_argument("--workload", default="grid",
                    choices=["grid", "points", "ensemble", "incompr", "adjoint",
-                            "krige"],
+                            "krige", "vario"],
                    help="grid: the headline (3-D Exponential, 256^3, 2000 "
                         "modes); the others are the remaining BASELINE "
                         "configurations")
@@ -627,6 +627,74 @@ def wl_krige(args, torch, gg, flush):
         gpu_launches=1)
 
 
+def wl_vario(args, torch, gg, flush):
+    """Omnidirectional Matheron variogram of 50 000 points uniform in
+    [0, 1000]^2 (one field), 40 bins up to 400: 1.25e9 point pairs per step;
+    plus the axis variogram of a 256^3 field.  Work unit: point pairs."""
+    import oracle
+    import gstools_gb300.variogram as gv
+    from gstools_gb300 import _native
+
+    rng = np.random.RandomState(20170519)
+    n, nb = 50_000, 40
+    pos = rng.uniform(0.0, 1000.0, (2, n))
+    f = rng.normal(size=(1, n))
+    edges = np.linspace(0.0, 400.0, nb + 1)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    dp, dfd, de = (torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+                   for a in (pos, f, edges))
+    vario = torch.zeros(nb, dtype=torch.float64, device=dev)
+    counts = torch.zeros(nb, dtype=torch.int64, device=dev)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def step():
+        _native.call("gst_vario_unstructured", 2, n, 1, p(dfd), nb, p(de), p(dp),
+                     ord("m"), ord("e"), p(vario), p(counts), stream)
+
+    t = _timed_events(torch, step, args.steps, args.warmup, flush)
+    pairs = n * (n - 1) / 2
+    sample = 3000
+    t0 = time.perf_counter()
+    go, co = oracle.c_vario_unstructured(f[:, :sample], edges, pos[:, :sample])
+    t_cpu = time.perf_counter() - t0
+    gs_, cs_ = gv.unstructured(f[:, :sample], edges, pos[:, :sample])
+    err = float(np.max(np.abs(gs_ - go) / np.maximum(np.abs(go), 1e-300)))
+    exact_counts = bool(np.array_equal(cs_, co))
+    t0 = time.perf_counter()
+    gv.unstructured(f, edges, pos)
+    te2e = time.perf_counter() - t0
+    fld = torch.from_numpy(rng.normal(size=(256, 256 * 256))).to(dev)
+    vs = torch.zeros(256, dtype=torch.float64, device=dev)
+
+    def axis_step():
+        _native.call("gst_vario_structured", 256, 256 * 256, p(fld),
+                     ctypes.c_void_p(0), ord("m"), p(vs), stream)
+
+    t_axis = _timed_events(torch, axis_step, args.steps, args.warmup, flush)
+    axis_pairs = 256 * 255 / 2 * 256 * 256
+    return dict(
+        metric="G point pairs/s of the empirical variogram (FP64)",
+        value=pairs / t / 1e9, unit="G pairs/s", n_gpus=1, steps=args.steps,
+        warmup=args.warmup, ms_per_step=t * 1e3, higher_is_better=True,
+        scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+        config={"workload": "vario_unstructured_2d_pts50000_bins40",
+                "pairs_per_step": pairs, "bins": nb},
+        error_vs_oracle={"max_rel": err, "counts_exact": exact_counts,
+                         "points": sample},
+        axis_variogram={"value": axis_pairs / t_axis / 1e9, "unit": "G pairs/s",
+                        "ms": t_axis * 1e3, "field": [256, 256, 256]},
+        cpu_baseline={"value": sample * (sample - 1) / 2 / t_cpu / 1e9,
+                      "unit": "G pairs/s", "cores": oracle.num_threads(),
+                      "kind": "port",
+                      "sample": f"{sample} points (the restated loop runs the "
+                                "bins outermost, as the reference's does)"},
+        e2e={"value": pairs / te2e / 1e9, "unit": "G pairs/s",
+             "h2d_bytes_per_step": int(pos.nbytes + f.nbytes + edges.nbytes),
+             "d2h_bytes_per_step": int(nb * 16)},
+        gpu_launches=2)
+
+
 def wl_points(args, torch, gg, flush):
     """2-D Gaussian, var 1, len_scale 10, 1000 modes (reference RNG, seed
     20170519), 100 000 points uniform in [0, 100]^2."""
@@ -920,6 +988,7 @@ def run_workload(args):
     build.build()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     fn = {"points": wl_points, "ensemble": wl_ensemble, "krige": wl_krige,
+          "vario": wl_vario,
           "incompr": wl_incompr, "adjoint": wl_adjoint}[args.workload]
     clocks = Clocks(0)
     clocks.start()

@@ -103,6 +103,12 @@ SIGNATURES = {
                                         _ptr, _ptr, _ptr, _ptr, _ptr, _ptr]),
     "gst_calc_field_krige": (_c_int, [_i64, _i64, _ptr, _ptr, _ptr, _ptr, _ptr,
                                       _ptr]),
+    "gst_vario_unstructured": (_c_int, [_c_int, _i64, _i64, _ptr, _i64, _ptr, _ptr,
+                                        _c_int, _c_int, _ptr, _ptr, _ptr]),
+    "gst_vario_directional": (_c_int, [_c_int, _i64, _i64, _ptr, _i64, _ptr, _ptr,
+                                       _i64, _ptr, _dbl, _dbl, _c_int, _c_int,
+                                       _ptr, _ptr, _ptr]),
+    "gst_vario_structured": (_c_int, [_i64, _i64, _ptr, _ptr, _c_int, _ptr, _ptr]),
     "gst_philox4x64_fill": (_c_int, [ctypes.c_uint64, ctypes.c_uint64, _i64,
                                      ctypes.c_uint64, _ptr, _ptr]),
     "gst_peak_probe": (_c_int, [_c_int, _i64, _ptr, ctypes.POINTER(_dbl),

@@ -10,12 +10,16 @@ to the reference.  Kriging is routed the same way: ``Krige._summate``
 (src/gstools/krige/base.py:307-320) calls the module globals
 ``_calc_field_krige`` / ``_calc_field_krige_and_variance`` (:42-60), which
 :func:`install` rebinds in ``gstools.krige.base`` when that module is
-importable.
+importable, and the variogram estimators likewise: ``vario_estimate`` /
+``vario_estimate_axis`` call ``_unstructured``, ``_directional``,
+``_structured`` and ``_ma_structured`` (src/gstools/variogram/
+variogram.py:48-124) in ``gstools.variogram.variogram``.
 """
 
 import sys
 
 from . import config
+from . import variogram as _vario
 from .krige import calc_field_krige, calc_field_krige_and_variance
 from .summator import summate, summate_fourier, summate_incompr
 
@@ -23,6 +27,7 @@ _saved = {}
 
 _NAMES = ("_summate", "_summate_incompr", "_summate_fourier")
 _KRIGE_NAMES = ("_calc_field_krige", "_calc_field_krige_and_variance")
+_VARIO_NAMES = ("_unstructured", "_directional", "_structured", "_ma_structured")
 
 
 def _generator_module(module=None):
@@ -46,7 +51,19 @@ def _krige_module(module=None):
     return mod
 
 
-def install(module=None, precision=None, krige_module=None):
+def _vario_module(module=None):
+    if module is not None:
+        return module
+    mod = sys.modules.get("gstools.variogram.variogram")
+    if mod is None:
+        try:
+            import gstools.variogram.variogram as mod  # noqa: F811
+        except ImportError:
+            return None
+    return mod
+
+
+def install(module=None, precision=None, krige_module=None, vario_module=None):
     """Route the reference's summation and kriging calls to the GPU kernels.
 
     ``module`` defaults to ``gstools.field.generator`` and ``krige_module``
@@ -93,13 +110,42 @@ def install(module=None, precision=None, krige_module=None):
 
         kmod._calc_field_krige = _calc_field_krige
         kmod._calc_field_krige_and_variance = _calc_field_krige_and_variance
+
+    vmod = _vario_module(vario_module)
+    if vmod is not None:
+        if id(vmod) not in _saved:
+            _saved[id(vmod)] = {n: getattr(vmod, n) for n in _VARIO_NAMES}
+
+        def _unstructured(field, bin_edges, pos, estimator_type="m",
+                          distance_type="e", num_threads=None):
+            return _vario.unstructured(field, bin_edges, pos, estimator_type,
+                                       distance_type, num_threads)
+
+        def _directional(field, bin_edges, pos, direction,
+                         angles_tol=3.141592653589793 / 8.0, bandwidth=-1.0,
+                         separate_dirs=False, estimator_type="m",
+                         num_threads=None):
+            return _vario.directional(field, bin_edges, pos, direction,
+                                      angles_tol, bandwidth, separate_dirs,
+                                      estimator_type, num_threads)
+
+        def _structured(field, estimator_type="m", num_threads=None):
+            return _vario.structured(field, estimator_type, num_threads)
+
+        def _ma_structured(field, mask, estimator_type="m", num_threads=None):
+            return _vario.ma_structured(field, mask, estimator_type, num_threads)
+
+        vmod._unstructured = _unstructured
+        vmod._directional = _directional
+        vmod._structured = _structured
+        vmod._ma_structured = _ma_structured
     return mod
 
 
-def uninstall(module=None, krige_module=None):
+def uninstall(module=None, krige_module=None, vario_module=None):
     """Restore the functions that :func:`install` replaced."""
     mod = _generator_module(module)
-    for m in (mod, _krige_module(krige_module)):
+    for m in (mod, _krige_module(krige_module), _vario_module(vario_module)):
         if m is None:
             continue
         saved = _saved.pop(id(m), None)

@@ -342,6 +342,35 @@ int gst_calc_field_krige(int64_t n_cond, int64_t n_pts, const double *krig_mat,
                          const double *krig_vecs, const double *cond, double *field,
                          double *error, void *stream);
 
+/* ----------------------------------------------------------------------- */
+/* Empirical variograms.  Replace gstools-cython's variogram kernels        */
+/* unstructured, directional, structured and ma_structured (imported        */
+/* src/gstools/variogram/variogram.py:14-17, called through the wrappers at */
+/* :48-124 from vario_estimate / vario_estimate_axis).  estimator 'm'       */
+/* (Matheron) or 'c' (Cressie); distance_type 'e' (Euclidean) or 'h'         */
+/* (haversine, dim 2: latitude and longitude in degrees, bins in radians).  */
+/* f (f_max x n fields; NaN = no data), pos (dim x n), bin_edges (n_bins + */
+/* 1, non-decreasing) and directions (n_dirs x dim unit vectors) are device */
+/* pointers; vario / counts (n_bins, or n_dirs x n_bins) device outputs,    */
+/* counts int64.  Pairs are binned exactly as the reference bins them       */
+/* (edge <= distance < next edge); sums are FP64 in another order (equal   */
+/* within rounding), counts exact.                                          */
+/* ----------------------------------------------------------------------- */
+int gst_vario_unstructured(int dim, int64_t n, int64_t f_max, const double *f,
+                           int64_t n_bins, const double *bin_edges, const double *pos,
+                           int estimator, int distance_type, double *vario,
+                           int64_t *counts, void *stream);
+int gst_vario_directional(int dim, int64_t n, int64_t f_max, const double *f,
+                          int64_t n_bins, const double *bin_edges, const double *pos,
+                          int64_t n_dirs, const double *directions, double angles_tol,
+                          double bandwidth, int separate_dirs, int estimator,
+                          double *vario, int64_t *counts, void *stream);
+/* Variogram along axis 0 of f (n0 x rest, row-major), lags 0 .. n0 - 1;   */
+/* mask (n0 x rest bytes, nonzero = masked) may be NULL.  Deterministic.    */
+int gst_vario_structured(int64_t n0, int64_t rest, const double *f,
+                         const unsigned char *mask, int estimator, double *vario,
+                         void *stream);
+
 /* Operand format of the tensor-core grid path's split GEMM (hi*hi + hi*lo +
  * lo*hi): GST_TC_F16 (default; FP16 products at twice the TF32 rate, the
  * amplitudes normalised by a power of two) or GST_TC_TF32.  Both keep 10

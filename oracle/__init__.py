@@ -16,6 +16,8 @@ Two independent restatements of the reference formulas
   numpy witness used to cross-check the C oracle;
 * ``c_krige`` / ``np_krige``: the kriging kernels of gstools-cython
   (``krige_oracle.c``) and a numpy witness;
+* ``c_vario_unstructured`` / ``c_vario_directional`` / ``c_vario_structured``:
+  the variogram estimators of gstools-cython (``vario_oracle.c``);
 * ``c_sample_modes`` / ``c_philox4x64``: the C restatement of the device
   spectral sampler (``sample_oracle.c``), its Philox stream pinned to numpy's
   Philox bit generator by the tests.
@@ -30,6 +32,9 @@ from .oracle import (  # noqa: F401
     c_summate,
     c_summate_fourier,
     c_summate_incompr,
+    c_vario_directional,
+    c_vario_structured,
+    c_vario_unstructured,
     library_path,
     num_threads,
     np_krige,

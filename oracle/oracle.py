@@ -7,6 +7,9 @@ Every function here restates the reference's formulas:
 * summate_fourier  -- src/gstools/field/generator.py:682-689
 * krige            -- calc_field_krige(_and_variance) of gstools-cython, called
                       by src/gstools/krige/base.py:42-60, 307-320
+* vario_*          -- the variogram estimators of gstools-cython (unstructured,
+                      directional, structured, ma_structured), called by
+                      src/gstools/variogram/variogram.py:48-124
 * sample_modes     -- the device spectral sampler of
                       gstools_gb300/csrc/gst_sampling.cu (Philox4x64-10
                       stream, sphere formulas of src/gstools/random/rng.py:
@@ -37,7 +40,8 @@ def library_path():
 def build(force=False):
     """Compile the C oracle with its Makefile (gcc, OpenMP)."""
     srcs = [os.path.join(_HERE, f)
-            for f in ("summate_oracle.c", "sample_oracle.c", "krige_oracle.c")]
+            for f in ("summate_oracle.c", "sample_oracle.c", "krige_oracle.c",
+                      "vario_oracle.c")]
     out = library_path()
     if (
         not force
@@ -71,6 +75,18 @@ def _load():
             u64 = ctypes.c_uint64
             lib.oracle_philox4x64.restype = None
             lib.oracle_philox4x64.argtypes = [u64] * 6 + [ctypes.POINTER(u64)]
+            ip = ctypes.POINTER(i64)
+            ch = ctypes.c_char
+            lib.oracle_vario_unstructured.restype = ctypes.c_int
+            lib.oracle_vario_unstructured.argtypes = [
+                ctypes.c_int, i64, i64, dp, i64, dp, dp, ch, ch, dp, ip]
+            lib.oracle_vario_directional.restype = ctypes.c_int
+            lib.oracle_vario_directional.argtypes = [
+                ctypes.c_int, i64, i64, dp, i64, dp, dp, i64, dp, ctypes.c_double,
+                ctypes.c_double, ctypes.c_int, ch, dp, ip]
+            lib.oracle_vario_structured.restype = ctypes.c_int
+            lib.oracle_vario_structured.argtypes = [
+                i64, i64, dp, ctypes.POINTER(ctypes.c_ubyte), ch, dp]
             lib.oracle_krige.restype = ctypes.c_int
             lib.oracle_krige.argtypes = [i64, i64, dp, dp, dp, dp, dp]
             lib.oracle_sample_modes.restype = ctypes.c_int
@@ -255,3 +271,74 @@ def np_krige(krig_mat, krig_vecs, cond):
     amv = np.abs(m) @ np.abs(v)
     return ((c * mv).sum(axis=0), (v * mv).sum(axis=0),
             ((np.abs(c) + np.abs(v)) * amv).sum(axis=0))
+
+
+def _est(estimator_type):
+    e = str(estimator_type)
+    if e not in ("m", "c"):
+        raise ValueError(f"unknown estimator type {estimator_type!r}")
+    return e.encode()
+
+
+def c_vario_unstructured(f, bin_edges, pos, estimator_type="m",
+                         distance_type="e", num_threads=None):
+    """gstools-cython's ``variogram.unstructured``: (variogram, counts)."""
+    pos = _f64(np.atleast_2d(pos))
+    dim, n = pos.shape
+    f = _f64(np.atleast_2d(f)).reshape(-1, n)
+    edges = _f64(bin_edges).reshape(-1)
+    nb = max(edges.size - 1, 0)
+    vario = np.zeros(nb)
+    counts = np.zeros(nb, dtype=np.int64)
+    dist = str(distance_type)
+    if dist not in ("e", "h"):
+        raise ValueError(f"unknown distance type {distance_type!r}")
+    rc = _load().oracle_vario_unstructured(
+        dim, n, f.shape[0], _ptr(f), nb, _ptr(edges), _ptr(pos), _est(estimator_type),
+        dist.encode(), _ptr(vario), counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    if rc:
+        raise ValueError(f"oracle_vario_unstructured failed with code {rc}")
+    return vario, counts
+
+
+def c_vario_directional(f, bin_edges, pos, direction, angles_tol=np.pi / 8.0,
+                        bandwidth=-1.0, separate_dirs=False, estimator_type="m",
+                        num_threads=None):
+    """gstools-cython's ``variogram.directional``: (variogram, counts),
+    each (directions, bins)."""
+    pos = _f64(np.atleast_2d(pos))
+    dim, n = pos.shape
+    f = _f64(np.atleast_2d(f)).reshape(-1, n)
+    edges = _f64(bin_edges).reshape(-1)
+    dirs = _f64(np.atleast_2d(direction)).reshape(-1, dim)
+    nb = max(edges.size - 1, 0)
+    vario = np.zeros((dirs.shape[0], nb))
+    counts = np.zeros((dirs.shape[0], nb), dtype=np.int64)
+    rc = _load().oracle_vario_directional(
+        dim, n, f.shape[0], _ptr(f), nb, _ptr(edges), _ptr(pos), dirs.shape[0],
+        _ptr(dirs), float(angles_tol), float(bandwidth), int(bool(separate_dirs)),
+        _est(estimator_type), _ptr(vario),
+        counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    if rc:
+        raise ValueError(f"oracle_vario_directional failed with code {rc}")
+    return vario, counts
+
+
+def c_vario_structured(f, estimator_type="m", num_threads=None, mask=None):
+    """gstools-cython's ``variogram.structured`` / ``ma_structured``:
+    the variogram along axis 0 of f (n0, ...), lags 0 .. n0 - 1."""
+    f = _f64(f)
+    n0 = f.shape[0] if f.ndim else 1
+    f = f.reshape(n0, -1)
+    m = None
+    if mask is not None:
+        m = np.ascontiguousarray(np.asarray(mask, dtype=bool).reshape(n0, -1),
+                                 dtype=np.uint8)
+    vario = np.zeros(n0)
+    rc = _load().oracle_vario_structured(
+        n0, f.shape[1], _ptr(f),
+        m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)) if m is not None else None,
+        _est(estimator_type), _ptr(vario))
+    if rc:
+        raise ValueError(f"oracle_vario_structured failed with code {rc}")
+    return vario

@@ -247,6 +247,76 @@ def reference_goldens(gs):
         ck.calc_field_krige_and_variance = orig
         kb._calc_field_krige_and_variance = kb_orig
 
+    # variograms: the arrays vario_estimate / vario_estimate_axis hand to
+    # gstools-cython's kernels (setups of tests/test_variogram_unstructured.py
+    # and test_variogram_structured.py), with the oracle's results
+    import gstools.variogram.variogram as vv
+
+    calls = []
+    saved = {n: getattr(vv, n) for n in ("unstructured_c", "directional_c",
+                                         "structured_c", "ma_structured_c")}
+
+    def recorder(name):
+        fct = saved[name]
+
+        def run(*args, **kwargs):
+            res = fct(*args, **kwargs)
+            calls.append((name, args, kwargs, res))
+            return res
+        return run
+
+    for n in saved:
+        setattr(vv, n, recorder(n))
+    try:
+        x = np.arange(1, 11, 1, dtype=np.double)
+        z = np.array((41.2, 40.2, 39.7, 39.2, 40.1, 38.3, 39.1, 40.0, 41.1, 40.3))
+        _, gam = gs.vario_estimate([x], z, np.arange(1, 11, 1.0))
+        check(gam[0], 0.4917, "vario_1d[0]", places=4)
+        check(gam[1], 0.7625, "vario_1d[1]", places=4)
+        rng = np.random.RandomState(1479373475)
+        xs, ys = rng.uniform(0, 100, 800), rng.uniform(0, 100, 800)
+        fld = rng.normal(0, 2.0, size=(2, 800))
+        fld[1, ::17] = np.nan
+        gs.vario_estimate((xs, ys), fld, np.linspace(0, 40, 21))
+        gs.vario_estimate((xs, ys), fld[0], np.linspace(0, 40, 21),
+                          estimator="cressie")
+        grid = np.arange(10.0)
+        f3 = rng.normal(size=(10, 10, 10))
+        f3m = np.ma.array(f3, mask=np.abs(f3) < 0.1)
+        gs.vario_estimate((grid, grid, grid), f3m, range(10),
+                          direction=((1, 0, 0), (0, 1, 0), (0, 0, 1)),
+                          bandwidth=0.25, mesh_type="structured")
+        gs.vario_estimate((grid[:8], grid), f3[:8, :, 0], range(0, 10, 2),
+                          angles=np.pi / 4, mesh_type="structured")
+        for ax in ("x", "y", "z"):
+            gs.vario_estimate_axis(f3m, ax)
+        gs.vario_estimate_axis(f3, "y", estimator="cressie")
+        lat, lon = rng.uniform(-60, 60, 300), rng.uniform(-180, 180, 300)
+        gs.vario_estimate((lat, lon), rng.normal(size=300), np.linspace(0, 2000, 11),
+                          latlon=True, geo_scale=gs.KM_SCALE)
+    finally:
+        for n, fct in saved.items():
+            setattr(vv, n, fct)
+    for i, (name, args, kwargs, res) in enumerate(calls):
+        key = f"vario_{i:02d}_{name[:-2]}"
+        if name in ("unstructured_c", "directional_c"):
+            names = ["f", "bin_edges", "pos"] + (
+                ["direction", "angles_tol", "bandwidth", "separate_dirs",
+                 "estimator_type"] if name == "directional_c" else
+                ["estimator_type", "distance_type"])
+        else:
+            names = ["f", "mask", "estimator_type"] if name == "ma_structured_c" \
+                else ["f", "estimator_type"]
+        vals = dict(zip(names, args))
+        vals.update(kwargs)
+        vals.pop("num_threads", None)
+        for k, v in vals.items():
+            out[f"{key}/{k}"] = np.asarray(v)
+        if isinstance(res, tuple):
+            out[f"{key}/vario"], out[f"{key}/counts"] = (np.asarray(r) for r in res)
+        else:
+            out[f"{key}/vario"] = np.asarray(res)
+
     # tests/test_rng.py:20-37: normal streams of RNG(19031977)
     rng = RNG(seed)
     z1 = rng.random.normal(size=100)

@@ -14,12 +14,17 @@ reference's own RNG, covariance models and SRF/RandMeth code drive the oracle.
 """
 
 import os
+
+import numpy as np
 import sys
 import types
 
 REFERENCE_SRC = os.environ.get(
     "GSTOOLS_REFERENCE_SRC", "/root/reference/src"
 )
+
+
+REF_TESTS = os.path.join(os.path.dirname(REFERENCE_SRC), "tests")
 
 
 def available():
@@ -50,9 +55,13 @@ def _install_stubs():
             oracle.c_summate_fourier(f, m, z1, z2, p)
         )
         vario = types.ModuleType("gstools_cython.variogram")
-        for name in ("directional", "ma_structured", "structured",
-                     "unstructured"):
-            setattr(vario, name, _unavailable(f"variogram.{name}"))
+        vario.unstructured = oracle.c_vario_unstructured
+        vario.directional = oracle.c_vario_directional
+        vario.structured = (lambda f, estimator_type="m", num_threads=None:
+                            oracle.c_vario_structured(f, estimator_type))
+        vario.ma_structured = (
+            lambda f, mask, estimator_type="m", num_threads=None:
+            oracle.c_vario_structured(f, estimator_type, mask=mask))
         krige = types.ModuleType("gstools_cython.krige")
         krige.calc_field_krige = lambda m, v, c, num_threads=None: (
             oracle.c_krige(m, v, c, with_error=False)
@@ -68,18 +77,69 @@ def _install_stubs():
             "gstools_cython.krige": krige,
         })
     if "emcee" not in sys.modules:
+        # emcee is absent: a small stand-in with the same interface and the
+        # affine-invariant stretch move (Goodman and Weare, Comm. App. Math.
+        # Comp. Sci. 5(1), 2010), so the reference's MCMC radius sampling
+        # (src/gstools/random/rng.py:38-103) runs.  Its random stream is not
+        # emcee's: samples follow the right law, but literal values drawn
+        # through MCMC differ from the reference's.
         emcee = types.ModuleType("emcee")
         state = types.ModuleType("emcee.state")
 
-        class _Missing:
-            def __init__(self, *args, **kwargs):
-                raise NotImplementedError(
-                    "emcee is not available: MCMC spectral sampling cannot "
-                    "run here; use sampling='inversion'"
-                )
+        class State:
+            def __init__(self, coords, copy=False):
+                src = coords.coords if isinstance(coords, State) else coords
+                self.coords = np.array(src, dtype=float, copy=True)
+                self.random_state = getattr(coords, "random_state", None)
 
-        emcee.EnsembleSampler = _Missing
-        state.State = _Missing
+        class EnsembleSampler:
+            def __init__(self, nwalkers, ndim, log_prob_fn, vectorize=False,
+                         a=2.0):
+                self.nwalkers, self.ndim, self.a = nwalkers, ndim, a
+                self.log_prob = log_prob_fn
+                self.vectorize = vectorize
+                self._chain = []
+
+            def _lp(self, x):
+                if self.vectorize:
+                    return np.asarray(self.log_prob(x), dtype=float).reshape(-1)
+                return np.array([self.log_prob(v) for v in x], dtype=float)
+
+            def run_mcmc(self, initial_state, nsteps, **kwargs):
+                st = initial_state if isinstance(initial_state, State) else \
+                    State(initial_state)
+                rng = np.random.RandomState()
+                if st.random_state is not None:
+                    rng.set_state(st.random_state)
+                x = st.coords.reshape(self.nwalkers, self.ndim).copy()
+                lp = self._lp(x)
+                half = self.nwalkers // 2
+                groups = (np.arange(half), np.arange(half, self.nwalkers))
+                for _ in range(int(nsteps)):
+                    for g in (0, 1):
+                        s_idx, c_idx = groups[g], groups[1 - g]
+                        z = ((self.a - 1.0) * rng.rand(len(s_idx)) + 1.0) ** 2 / self.a
+                        c = x[c_idx[rng.randint(len(c_idx), size=len(s_idx))]]
+                        prop = c + z[:, None] * (x[s_idx] - c)
+                        lp_new = self._lp(prop)
+                        ln_ratio = (self.ndim - 1.0) * np.log(z) + lp_new - lp[s_idx]
+                        acc = np.log(rng.rand(len(s_idx))) < ln_ratio
+                        x[s_idx[acc]] = prop[acc]
+                        lp[s_idx[acc]] = lp_new[acc]
+                    self._chain.append(x.copy())
+                out = State(x)
+                out.random_state = rng.get_state()
+                return out
+
+            def reset(self):
+                self._chain = []
+
+            def get_chain(self, flat=False, **kwargs):
+                chain = np.array(self._chain)
+                return chain.reshape(-1, self.ndim) if flat else chain
+
+        emcee.EnsembleSampler = EnsembleSampler
+        state.State = State
         emcee.state = state
         sys.modules.update({"emcee": emcee, "emcee.state": state})
     if "hankel" not in sys.modules:
