@@ -441,7 +441,8 @@ def run_ours(args):
     if path == "tensor":
         peak, peak_src = tensor_peak()
         alg = 4.0 * work / t_main / 1e12
-        n_pad = -(-N_MODES // 16) * 16
+        mps = 32 if args.operands == "f16" else 16   # modes per pipeline stage
+        n_pad = -(-N_MODES // mps) * mps
         executed = 12.0 * n_pad * (-(-n // 256) * 256) * n * n / t_main / 1e12
         op_note = ("FP16 MMAs (3xFP16 split, padded), FP16 runs at the bf16 "
                    "rate" if args.operands == "f16" else

@@ -69,13 +69,19 @@ constexpr int kColsPerThread = 64;   // epilogue: a quarter row of 256 columns
 // w = z1 - i z2 and put back in the epilogue).
 enum OperandKind { kOpTf32 = GST_TC_TF32, kOpF16 = GST_TC_F16 };
 
-// Modes per pipeline stage: 16 for 3-D grids; 8 for 2-D grids, whose
-// per-CTA w*Ex slice (128 distinct x rows) is 16 times larger.
-__host__ __device__ constexpr int modes_per_stage(int ty) { return ty == 1 ? 8 : 16; }
+// Modes per pipeline stage: 32 (FP16) / 16 (TF32) for 3-D grids, half that
+// for 2-D grids, whose per-CTA w*Ex slice (128 distinct x rows) is 16 times
+// larger.  A stage is 4 MMA K-steps per operand format for 3-D grids, so a
+// stage is 70 KB of shared memory either way (a 3-deep ring); measured on the
+// 256^3 workload, 32-mode FP16 stages contract 16 % faster than 16-mode ones
+// (half the barrier round trips per mode).
+__host__ __device__ constexpr int modes_per_stage(int ty, int op) {
+    return (ty == 1 ? 8 : 16) * (op == kOpF16 ? 2 : 1);
+}
 // Modes per MMA K-step (32 bytes of K per row: 8 TF32 or 16 FP16 reals).
 __host__ __device__ constexpr int modes_per_kstep(int op) { return op == kOpF16 ? 8 : 4; }
 __host__ __device__ constexpr int ksteps_for(int ty, int op) {
-    return modes_per_stage(ty) / modes_per_kstep(op);
+    return modes_per_stage(ty, op) / modes_per_kstep(op);
 }
 __host__ __device__ constexpr int elem_bytes(int op) { return op == kOpF16 ? 2 : 4; }
 // Modes accumulated per TMEM chunk before the epilogue warps add the chunk
@@ -493,7 +499,7 @@ template <int TY, int OP>
 struct StageLayout {
     static constexpr int TX = kCtaRows / TY;
     static constexpr int KS = ksteps_for(TY, OP);
-    static constexpr int kModesPerStage = modes_per_stage(TY);
+    static constexpr int kModesPerStage = modes_per_stage(TY, OP);
     static constexpr int kChunkStages = chunk_modes(OP) / kModesPerStage;
     static constexpr int kAStageBytes = KS * 2 * kBlockBytes;
     static constexpr int kBStageBytes = KS * 2 * kBlockBytes;   // per CTA
@@ -1043,7 +1049,7 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
     g.blocks[2] = p.pair_blocks[2];
     g.op = op;
     g.ksteps = ksteps_for(p.ty, op);
-    const int mps = modes_per_stage(p.ty);
+    const int mps = modes_per_stage(p.ty, op);
     g.n_stages = ceil_div(n_modes, mps);
     g.n_modes = n_modes;
     if (2 * p.pair_blocks[0] * p.pair_blocks[1] * p.pair_blocks[2] > 0x7fffffffLL)
@@ -1072,7 +1078,7 @@ int run_tables(const GridPlan &p, const double *axes, const double *cov,
                const double *z1, const double *z2, unsigned char *ws,
                cudaStream_t s, Weight wgt = Weight{kWeightNone, 0, 0, nullptr}) {
     const GridGeom &g = p.g;
-    const int64_t n_pad_modes = g.n_stages * modes_per_stage(p.ty);
+    const int64_t n_pad_modes = g.n_stages * modes_per_stage(p.ty, g.op);
     ModeSplit *modes = reinterpret_cast<ModeSplit *>(ws + p.modes_off);
     float4 *points = reinterpret_cast<float4 *>(ws + p.points_off);
     unsigned int *amp = reinterpret_cast<unsigned int *>(ws + p.amp_off);
