@@ -52,7 +52,7 @@ VAR = 2.0
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 # DRAM bytes (read + write) of one contraction launch on this workload, from
 # the ncu capture summarised in profiles/grid_tc_kernel_exp3d_grid256.md.
-TC_DRAM_BYTES_PER_LAUNCH = 31.1e6
+TC_DRAM_BYTES_PER_LAUNCH = 34.6e6
 
 
 def parse():
@@ -452,8 +452,10 @@ def run_ours(args):
                 "unit": "TFLOP/s", "frac": alg / peak,
                 "traffic": TC_DRAM_BYTES_PER_LAUNCH,
                 "traffic_note": ("dram read+write bytes per contraction "
-                                 "launch (ncu); the 67 MB float32 field "
-                                 "stays in L2 at launch end"),
+                                 "launch (ncu full capture of this build, "
+                                 "profiles/grid_tc_kernel_exp3d_grid256.md); "
+                                 "the 67 MB float32 field stays in L2 at "
+                                 "launch end"),
                 "kernel": "grid_tc_kernel (contraction)",
                 "kernel_ms": t_main * 1e3,
                 "note": (f"achieved = 4 algorithmic flops per mode*point "
