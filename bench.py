@@ -452,8 +452,7 @@ def run_ours(args):
                 "unit": "TFLOP/s", "frac": alg / peak,
                 "traffic": TC_DRAM_BYTES_PER_LAUNCH,
                 "traffic_note": ("dram read+write bytes per contraction "
-                                 "launch (ncu full capture of this build, "
-                                 "profiles/grid_tc_kernel_exp3d_grid256.md); "
+                                 "launch (ncu full capture of this build); "
                                  "the 67 MB float32 field stays in L2 at "
                                  "launch end"),
                 "kernel": "grid_tc_kernel (contraction)",
