@@ -71,8 +71,10 @@ def parse():
                    choices=["grid", "points", "ensemble", "incompr", "adjoint",
                             "krige", "vario"],
                    help="grid: the headline (3-D Exponential, 256^3, 2000 "
-                        "modes); the others are the remaining BASELINE "
-                        "configurations")
+                        "modes); points: 2-D Gaussian, 100k points; ensemble: "
+                        "512 Matern realizations; incompr: 3-D incompressible "
+                        "field, 192^3; adjoint: gradients of a 3-D field; "
+                        "krige: ordinary kriging; vario: empirical variogram")
     return p.parse_args()
 
 
@@ -518,8 +520,8 @@ def run_ours(args):
 
 
 # ---------------------------------------------------------------------------
-# The other BASELINE configurations (not the headline; run explicitly with
-# --workload).  Each prints one JSON line with the same timing rules.
+# The other workloads (not the headline; run explicitly with --workload).
+# Each prints one JSON line with the same timing rules.
 # ---------------------------------------------------------------------------
 
 def _timed_events(torch, fn, steps, warmup, flush):

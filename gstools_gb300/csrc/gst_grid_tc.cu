@@ -55,7 +55,6 @@ namespace {
 constexpr int kThreads = 576;
 constexpr int kGenThreads = 512;      // warps 2-17
 constexpr int kCtaRows = 128;         // (x, y) rows held by each CTA
-constexpr int kPairRows = 256;        // rows of one CTA pair (MMA M)
 constexpr int kTileCols = 256;        // z points per pair tile (MMA N)
 constexpr int kCtaCols = 128;         // z rows of B held by each CTA
 constexpr int kBlockBytes = 128 * 32;  // 128 rows x 32 bytes of K (one K-step)
