@@ -383,6 +383,32 @@ def run_ours(args):
         others[f"tensor_{alt}_operands"] = world * work / max_over_ranks(
             statistics.mean(t_alt)) / 1e9
         del alt_ws
+        # the 2-D form of the tensor-core path: 2-D Gaussian modes (1000,
+        # reference RNG, fixture) on an 8192^2 grid, float32 output
+        wl = np.load(os.path.join(ROOT, "tests", "golden", "workloads.npz"))
+        cov2, z12, z22 = wl["gau2d/cov"], wl["gau2d/z1"], wl["gau2d/z2"]
+        n2, m2 = 8192, cov2.shape[1]
+        lens2 = (ctypes.c_int64 * 4)(n2, n2, 1, 1)
+        t2 = [torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+              for a in (np.concatenate([np.arange(float(n2))] * 2), cov2, z12, z22)]
+        out2 = torch.empty((n2, n2), dtype=torch.float32, device=dev)
+        ws2_bytes = ctypes.c_size_t(0)
+        _native.call("gst_grid_tc_workspace_size", 2, m2, lens2,
+                     ctypes.byref(ws2_bytes))
+        ws2 = torch.empty(max(ws2_bytes.value, 1), dtype=torch.uint8, device=dev)
+
+        def tables2():
+            _native.call("gst_grid_tc_tables", 2, m2, lens2, p(t2[0]), p(t2[1]),
+                         p(t2[2]), p(t2[3]), p(ws2), ws2_bytes, sp)
+
+        def contract2():
+            _native.call("gst_grid_tc_contract", 2, m2, lens2, p(ws2), ws2_bytes,
+                         p(out2), _native.GST_OUT_F32, 1.0, sp)
+
+        t_2d, _ = timed([tables2, contract2], 5, 2)
+        others["tensor_2d_gau2d_grid8192_modes1000"] = world * m2 * n2 * n2 / \
+            max_over_ranks(statistics.mean(t_2d)) / 1e9
+        del ws2, out2
     slab = max(1, n // 16)
     lens64 = (ctypes.c_int64 * 4)(slab, n, n, 1)
     out64 = torch.empty((slab, n, n), dtype=torch.float64, device=dev)
