@@ -65,6 +65,9 @@ def parse():
     p.add_argument("--path", default="auto",
                    choices=["auto", "mixed", "tensor", "f64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--size", default="full", choices=["full", "small"],
+                   help="small: reduced problem sizes of the krige and vario "
+                        "workloads (for profiler captures)")
     p.add_argument("--operands", default="f16", choices=["f16", "tf32"],
                    help="operand format of the tensor-core split GEMM")
     p.add_argument("--workload", default="grid",
@@ -589,7 +592,7 @@ def wl_krige(args, torch, gg, flush):
     from scipy.spatial.distance import cdist
 
     rng = np.random.RandomState(20170519)
-    n_cond, n_pts = 1000, 65536
+    n_cond, n_pts = (1000, 65536) if args.size == "full" else (1000, 16384)
     cpos = rng.uniform(0.0, 500.0, (2, n_cond))
     tpos = rng.uniform(0.0, 500.0, (2, n_pts))
     cond = np.append(rng.normal(size=n_cond), 0.0)
@@ -641,7 +644,7 @@ def wl_krige(args, torch, gg, flush):
         value=flops / t / 1e9, unit="GFLOP/s", n_gpus=1, steps=args.steps,
         warmup=args.warmup, ms_per_step=t * 1e3, higher_is_better=True,
         scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
-        config={"workload": "ordinary_krige_exp2d_cond1000_pts65536",
+        config={"workload": f"ordinary_krige_exp2d_cond1000_pts{n_pts}",
                 "n_cond": k, "n_pts": n_pts},
         error_vs_oracle={"max_rel_to_term_scale": err, "points": sample},
         roofline={"bound": "fp64", "achieved": achieved, "peak": peak64,
@@ -666,7 +669,7 @@ def wl_vario(args, torch, gg, flush):
     from gstools_gb300 import _native
 
     rng = np.random.RandomState(20170519)
-    n, nb = 50_000, 40
+    n, nb = (50_000, 40) if args.size == "full" else (20_000, 40)
     pos = rng.uniform(0.0, 1000.0, (2, n))
     f = rng.normal(size=(1, n))
     edges = np.linspace(0.0, 400.0, nb + 1)
@@ -694,26 +697,27 @@ def wl_vario(args, torch, gg, flush):
     t0 = time.perf_counter()
     gv.unstructured(f, edges, pos)
     te2e = time.perf_counter() - t0
-    fld = torch.from_numpy(rng.normal(size=(256, 256 * 256))).to(dev)
-    vs = torch.zeros(256, dtype=torch.float64, device=dev)
+    na = 256 if args.size == "full" else 128
+    fld = torch.from_numpy(rng.normal(size=(na, na * na))).to(dev)
+    vs = torch.zeros(na, dtype=torch.float64, device=dev)
 
     def axis_step():
-        _native.call("gst_vario_structured", 256, 256 * 256, p(fld),
+        _native.call("gst_vario_structured", na, na * na, p(fld),
                      ctypes.c_void_p(0), ord("m"), p(vs), stream)
 
     t_axis = _timed_events(torch, axis_step, args.steps, args.warmup, flush)
-    axis_pairs = 256 * 255 / 2 * 256 * 256
+    axis_pairs = na * (na - 1) / 2 * na * na
     return dict(
         metric="G point pairs/s of the empirical variogram (FP64)",
         value=pairs / t / 1e9, unit="G pairs/s", n_gpus=1, steps=args.steps,
         warmup=args.warmup, ms_per_step=t * 1e3, higher_is_better=True,
         scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
-        config={"workload": "vario_unstructured_2d_pts50000_bins40",
+        config={"workload": f"vario_unstructured_2d_pts{n}_bins{nb}",
                 "pairs_per_step": pairs, "bins": nb},
         error_vs_oracle={"max_rel": err, "counts_exact": exact_counts,
                          "points": sample},
         axis_variogram={"value": axis_pairs / t_axis / 1e9, "unit": "G pairs/s",
-                        "ms": t_axis * 1e3, "field": [256, 256, 256]},
+                        "ms": t_axis * 1e3, "field": [na, na, na]},
         cpu_baseline={"value": sample * (sample - 1) / 2 / t_cpu / 1e9,
                       "unit": "G pairs/s", "cores": oracle.num_threads(),
                       "kind": "port",

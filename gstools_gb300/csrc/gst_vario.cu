@@ -49,23 +49,27 @@ __device__ __forceinline__ double haversine(double lat_j, double lon_j, double l
 }
 
 // Bin of distance `dist` given as its square d2 (exact sqrt on demand):
-// last i with edge[i] <= dist < edge[i + 1], or -1.
+// last i with edge[i] <= dist < edge[i + 1], or -1.  The search runs in
+// FP32 on the squared edges (GB300's FP64 rate is 1/64 of its FP32 rate);
+// within 2^-20 (relative) of a squared edge, where FP32 rounding could
+// change the order, the exact FP64 distance decides.
 __device__ __forceinline__ int find_bin(double d2, const double *edges,
-                                        const double *edges2, int n_bins,
+                                        const float *edges2f, int n_bins,
                                         double &dist, bool &have_dist) {
-    // coarse search on squared edges
     if (!(d2 >= 0.0)) return -1;
-    int lo = -1, hi = n_bins + 1;   // edges2[lo] <= d2 < edges2[hi] (virtual)
+    const float f2 = __double2float_rn(d2);
+    constexpr float kGuard = 9.5367431640625e-07f;   // 2^-20
+    // beyond the last edge: no bin (the common case for far pairs)
+    if (f2 > edges2f[n_bins] * (1.0f + kGuard)) return -1;
+    int lo = -1, hi = n_bins + 1;   // edges2f[lo] <= f2 < edges2f[hi] (virtual)
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
-        if (edges2[mid] <= d2) lo = mid; else hi = mid;
+        if (edges2f[mid] <= f2) lo = mid; else hi = mid;
     }
-    // near a squared edge the order of d2 and edge^2 may differ from the
-    // order of sqrt(d2) and edge: decide with the exact distance there
-    const double tol = 4.0 * 2.220446049250313e-16;
     bool near = false;
-    if (lo >= 0 && fabs(d2 - edges2[lo]) <= tol * edges2[lo]) near = true;
-    if (lo + 1 <= n_bins && fabs(d2 - edges2[lo + 1]) <= tol * edges2[lo + 1]) near = true;
+    if (lo >= 0 && fabsf(f2 - edges2f[lo]) <= kGuard * edges2f[lo]) near = true;
+    if (lo + 1 <= n_bins && fabsf(f2 - edges2f[lo + 1]) <= kGuard * edges2f[lo + 1])
+        near = true;
     if (near) {
         if (!have_dist) {
             dist = sqrt(d2);
@@ -107,8 +111,8 @@ __global__ void __launch_bounds__(kVarioThreads)
     const int nb = a.n_bins;
     const int nh = (a.d_max > 0 ? a.d_max : 1) * nb;
     double *edges = sh;
-    double *edges2 = edges + (nb + 1);
-    double *h_sum = edges2 + (nb + 1);
+    float *edges2f = reinterpret_cast<float *>(edges + (nb + 1));
+    double *h_sum = edges + 2 * (nb + 1);
     unsigned long long *h_cnt = reinterpret_cast<unsigned long long *>(h_sum + nh);
     // upper-triangle tile (tj <= tk) from the linear block index
     const int64_t t = blockIdx.x;
@@ -124,7 +128,7 @@ __global__ void __launch_bounds__(kVarioThreads)
         edges[i] = e;
         // non-positive edges lie below every distance: keep the squared
         // table monotonic
-        edges2[i] = e > 0.0 ? e * e : -1.0;
+        edges2f[i] = e > 0.0 ? __double2float_rn(e * e) : -1.0f;
     }
     for (int i = threadIdx.x; i < nh; i += blockDim.x) {
         h_sum[i] = 0.0;
@@ -163,7 +167,7 @@ __global__ void __launch_bounds__(kVarioThreads)
                 }
                 bin = (lo >= 0 && lo < nb) ? lo : -1;
             } else {
-                bin = find_bin(d2, edges, edges2, nb, dist, have_dist);
+                bin = find_bin(d2, edges, edges2f, nb, dist, have_dist);
             }
             if (bin < 0) continue;
             if (a.d_max == 0) {
