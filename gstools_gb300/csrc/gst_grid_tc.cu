@@ -403,9 +403,23 @@ __global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ mod
     const int64_t rows = pick3(g.blocks, axis) * tile;
     const int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (idx >= rows * n_pad_modes) return;
-    // axis points fastest: coalesced table writes, one mode per warp
-    const int64_t r = idx % rows;
-    const int64_t j = idx / rows;
+    // Points fastest (coalesced writes, one mode per warp), except axis x of
+    // 3-D grids: modes fastest within a stage, so each x row's modes of a
+    // stage are contiguous ([block][stage][point][mode]) and the generators
+    // load two modes of w*Ex per 16-byte load.  A warp reads two x rows
+    // there; the 16 Ey rows it reads (and the 32 x rows of a 2-D grid) stay
+    // point-fastest, which keeps those loads free of bank conflicts.
+    const bool x_modes_fastest = axis == 0 && g.tile[1] > 1;
+    int64_t r, j;
+    if (!x_modes_fastest) {
+        r = idx % rows;
+        j = idx / rows;
+    } else {
+        const int64_t stage = idx / (rows * mps);
+        const int64_t rem = idx % (rows * mps);
+        r = rem / mps;
+        j = stage * mps + rem % mps;
+    }
 
     float c = 0.0f, s = 0.0f;
     const bool live = (j < g.n_modes) && (r < pick3(g.n, axis));
@@ -433,7 +447,10 @@ __global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ mod
             re = ldexpf(fmaf(w1, c, w2 * s), -e);
             im = ldexpf(fmaf(w1, s, -w2 * c), -e);
         }
-        wx[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(re, im);
+        if (x_modes_fastest)
+            wx[((blk * g.n_stages + st) * tile + t) * mps + mm] = make_float2(re, im);
+        else
+            wx[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(re, im);
     } else if (axis == 1) {
         ey[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(c, s);
     } else {
@@ -787,11 +804,24 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int mm = m0 + sg * kRun / 2;        // first mode of the run
                 float x[kRun];
 #pragma unroll
-                for (int m = 0; m < kRun / 2; ++m) {
-                    const float2 p = swx[(mm + m) * TX + xl];
-                    const float2 e = sey[(mm + m) * TY + yl];
-                    x[2 * m] = fmaf(p.x, e.x, -p.y * e.y);
-                    x[2 * m + 1] = -fmaf(p.x, e.y, p.y * e.x);
+                for (int m = 0; m < kRun / 2; m += 2) {
+                    float2 p0, p1;
+                    if constexpr (TY > 1) {
+                        // two modes of w*Ex per load (mode-fastest rows)
+                        const float4 p2 = *reinterpret_cast<const float4 *>(
+                            swx + xl * kModesPerStage + mm + m);
+                        p0 = make_float2(p2.x, p2.y);
+                        p1 = make_float2(p2.z, p2.w);
+                    } else {
+                        p0 = swx[(mm + m) * TX + xl];
+                        p1 = swx[(mm + m + 1) * TX + xl];
+                    }
+                    const float2 e0 = sey[(mm + m) * TY + yl];
+                    const float2 e1 = sey[(mm + m + 1) * TY + yl];
+                    x[2 * m] = fmaf(p0.x, e0.x, -p0.y * e0.y);
+                    x[2 * m + 1] = -fmaf(p0.x, e0.y, p0.y * e0.x);
+                    x[2 * m + 2] = fmaf(p1.x, e1.x, -p1.y * e1.y);
+                    x[2 * m + 3] = -fmaf(p1.x, e1.y, p1.y * e1.x);
                 }
                 const int ksg = mm / kMpk;                // its K-step
                 const uint32_t o = core_offset(row, 2u * (mm % kMpk), OP);
