@@ -304,12 +304,14 @@ def run_ours(args):
 
     if path == "tensor":
         parts = [tc_tables, tc_contract]
-        launches_per_step = 2
+        # grid_prep_kernel + grid_tables_kernel, then zero_split_tiles_kernel
+        # (the 256 pair tiles leave a partial last wave) + grid_tc_kernel
+        launches_per_step = 4
         desc = (f"separable 3x{args.operands.upper()} tensor-core grid path "
                 f"(tables + contraction)")
     else:
         parts = [step_mixed]
-        launches_per_step = 2
+        launches_per_step = 2   # pack_modes_kernel + pointwise_kernel
         desc = "mixed-precision pointwise grid kernel"
 
     def timed(parts, steps, warmup):
