@@ -328,3 +328,34 @@ def test_tc_fourier_small_spectrum_factor(cuda_lib):
     got = gg.summate_fourier_grid(fac, cov, z1, z2, axes)
     d = (got - ref) / np.sqrt(np.sum(fac ** 2))
     assert np.sqrt(np.mean(d ** 2)) <= RMS_SIGMA and np.abs(d).max() <= MAX_SIGMA
+
+
+def test_tc_full_size_workload(cuda_lib, workloads):
+    """The 256^3 x 2000-mode Exponential workload at full size: the oracle at
+    4096 random grid points (bar of this file), and two size-independent
+    properties: scaling the amplitudes by a power of two scales the field
+    exactly (the FP16 normalisation takes out that power), and the field is
+    linear in (z_1, z_2) within the bar."""
+    import torch
+
+    cov = workloads["exp3d/isometrize"].T @ workloads["exp3d/cov"]
+    z1, z2 = workloads["exp3d/z1"], workloads["exp3d/z2"]
+    n, n_modes = 256, cov.shape[1]
+    axes = [np.arange(float(n))] * 3
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    dax = [t(a) for a in axes]
+    run = lambda a, b: gg.summate_grid(t(cov), t(a), t(b), dax, precision="mixed",
+                                       method="tensor", out_dtype="float32")
+    f = run(z1, z2)
+    rng = np.random.RandomState(4)
+    idx = rng.randint(0, n, size=(3, 4096))
+    ref = oracle.c_summate(cov, z1, z2, idx.astype(np.float64))
+    got = f[idx[0], idx[1], idx[2]].double().cpu().numpy()
+    rms, mx = errors(got, ref, n_modes, var=2.0)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (rms, mx)
+    f8 = run(8.0 * z1, 8.0 * z2)
+    assert torch.equal(f8, 8.0 * f)
+    za, zb = rng.normal(size=n_modes), rng.normal(size=n_modes)
+    fa, fb, fab = run(za, zb), run(z1 - za, z2 - zb), f
+    d = np.sqrt(1.0 / n_modes) * (fa + fb - fab).double().cpu().numpy()
+    assert np.sqrt(np.mean(d ** 2)) <= 2 * RMS_SIGMA
