@@ -493,7 +493,10 @@ def run_ours(args):
                 "note": (f"achieved = 4 algorithmic flops per mode*point "
                          f"(Re of a complex MAC) / contraction time; peak = "
                          f"{peak_src} dense bf16; the kernel executes "
-                         f"{executed:.0f} TFLOP/s of {op_note}")}
+                         f"{executed:.0f} TFLOP/s of {op_note}; the three-"
+                         f"product hi/lo split executes 3 MMA flops per "
+                         f"algorithmic flop, so frac is at most 1/3 (FP16) "
+                         f"or 1/6 (TF32)")}
     else:
         alg = 10.0 * work / t_main / 1e12
         roof = {"bound": "fp32", "achieved": alg, "peak": peaks["fp32_tflops"],
