@@ -222,6 +222,38 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def hbm_peak():
+    """Measured HBM copy bandwidth (GB/s), or None."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def peak_probe(torch, kind, iters):
+    """Best of three timed launches of gst_peak_probe (after one untimed):
+    0 FP32 FMA, 1 FP64 FMA (flop/s), 2 SFU sin (op/s), on the current stream."""
+    from gstools_gb300 import _native
+
+    sink = torch.zeros(256, dtype=torch.float32, device="cuda")
+    ops = ctypes.c_double(0.0)
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    sk = ctypes.c_void_p(sink.data_ptr())
+    _native.call("gst_peak_probe", kind, iters, sk, ctypes.byref(ops), sp)
+    best = 0.0
+    for _ in range(3):
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        _native.call("gst_peak_probe", kind, iters, sk, ctypes.byref(ops), sp)
+        ev1.record(stream)
+        ev1.synchronize()
+        best = max(best, ops.value / (ev0.elapsed_time(ev1) / 1e3))
+    return best
+
+
 def tensor_peak():
     """Measured dense bf16 tensor peak (TFLOP/s) and where it came from."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -452,25 +484,9 @@ def run_ours(args):
     d2h = res.nbytes
 
     # -- roofline of the dominant kernel -------------------------------------
-    sink = torch.zeros(256, dtype=torch.float32, device=dev)
-    ops = ctypes.c_double(0.0)
-
-    def probe(kind, iters):
-        best = 0.0
-        for _ in range(3):
-            ev0 = torch.cuda.Event(enable_timing=True)
-            ev1 = torch.cuda.Event(enable_timing=True)
-            ev0.record(stream)
-            _native.call("gst_peak_probe", kind, iters, p(sink),
-                         ctypes.byref(ops), sp)
-            ev1.record(stream)
-            ev1.synchronize()
-            best = max(best, ops.value / (ev0.elapsed_time(ev1) / 1e3))
-        return best
-
-    peaks = {"fp32_tflops": probe(0, 4096) / 1e12,
-             "fp64_tflops": probe(1, 64) / 1e12,
-             "sfu_tops": probe(2, 512) / 1e12}
+    peaks = {"fp32_tflops": peak_probe(torch, 0, 4096) / 1e12,
+             "fp64_tflops": peak_probe(torch, 1, 256) / 1e12,
+             "sfu_tops": peak_probe(torch, 2, 512) / 1e12}
     if path == "tensor":
         peak, peak_src = tensor_peak()
         alg = 4.0 * work / t_main / 1e12
@@ -618,31 +634,24 @@ def wl_krige(args, torch, gg, flush):
     step = lambda: gg.calc_field_krige_and_variance(dm, dv, dc)
     t = _timed_events(torch, step, args.steps, args.warmup, flush)
     f, e = step()
+    # the field alone: V^T (M^T c), one pass over V (HBM-bound)
+    t_field = _timed_events(torch, lambda: gg.calc_field_krige(dm, dv, dc),
+                            args.steps, args.warmup, flush)
+    field_bytes = 8.0 * (k * k + k * n_pts + n_pts)
+    hbm = hbm_peak()
+    f_only = gg.calc_field_krige(dm, dv, dc)
     sample = 512
     t0 = time.perf_counter()
     fo, eo = oracle.c_krige(mat, vecs[:, :sample], cond)
     t_cpu = time.perf_counter() - t0
     _, _, scale = oracle.np_krige(mat, vecs[:, :sample], cond)
     err = float(max(np.max(np.abs(f[:sample].cpu().numpy() - fo) / scale),
-                    np.max(np.abs(e[:sample].cpu().numpy() - eo) / scale)))
+                    np.max(np.abs(e[:sample].cpu().numpy() - eo) / scale),
+                    np.max(np.abs(f_only[:sample].cpu().numpy() - fo) / scale)))
     t0 = time.perf_counter()
     fe = gg.calc_field_krige_and_variance(mat, vecs, cond)
     te2e = time.perf_counter() - t0
-    peak64 = None
-    try:
-        sink = torch.zeros(256, dtype=torch.float32, device=dev)
-        ops = ctypes.c_double(0.0)
-        from gstools_gb300 import _native
-        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        _native.call("gst_peak_probe", 1, 64, ctypes.c_void_p(sink.data_ptr()),
-                     ctypes.byref(ops), stream)
-        e1.record()
-        e1.synchronize()
-        peak64 = ops.value / (e0.elapsed_time(e1) / 1e3) / 1e12
-    except Exception:  # noqa: BLE001 - the probe is informational here
-        pass
+    peak64 = peak_probe(torch, 1, 256) / 1e12
     achieved = flops / t / 1e12
     return dict(
         metric="GFLOP/s of the kriging field + variance (FP64)",
@@ -652,6 +661,11 @@ def wl_krige(args, torch, gg, flush):
         config={"workload": f"ordinary_krige_exp2d_cond1000_pts{n_pts}",
                 "n_cond": k, "n_pts": n_pts},
         error_vs_oracle={"max_rel_to_term_scale": err, "points": sample},
+        field_only={"ms": t_field * 1e3, "GB_per_s": field_bytes / t_field / 1e9,
+                    "hbm_frac_of_measured": (field_bytes / t_field / 1e9 / hbm
+                                             if hbm else None),
+                    "equivalent_GFLOP_per_s": flops / 2 / t_field / 1e9,
+                    "note": "calc_field_krige: V^T (M^T c), bytes = 8 (K^2 + K n + n)"},
         roofline={"bound": "fp64", "achieved": achieved, "peak": peak64,
                   "unit": "TFLOP/s",
                   "frac": achieved / peak64 if peak64 else None,

@@ -9,13 +9,17 @@
 //
 //     f_k = sum_i c_i (M v_k)_i,        e_k = sum_i v_ik (M v_k)_i,
 //
-// a K^2 n FP64 contraction.  Here one CTA owns 64 target points and walks the
-// rows of M in blocks of 64: the 64 x 64 block of M V is accumulated in
-// registers (4 x 4 per thread) from shared-memory tiles of M and V, and
-// reduced at once against c and the matching rows of V, so M V is never
-// stored.  Every partial sum is kept per thread in a fixed order and reduced
-// in a fixed order: results are deterministic.  GB300's FP64 FMA rate
-// (~1/64 of FP32) bounds the kernel.
+// a K^2 n FP64 contraction.  With the variance, one CTA owns 64 target
+// points and walks the rows of M in blocks of 64: the 64 x 64 block of M V is
+// accumulated in registers (4 x 4 per thread) from shared-memory tiles of M
+// and V, and reduced at once against c and the matching rows of V, so M V is
+// never stored.  GB300's FP64 FMA rate (~1/64 of FP32) bounds that kernel.
+// The field alone is f = (M^T c)^T V: the weights u = M^T c (K^2 flops) and
+// one pass over V (K n flops, bound by HBM) give it without the K^2 n
+// contraction; the sums run in another order than the nested loops, with the
+// same FP64 error bound (relative to sum_i |c_i| sum_j |M_ij| |v_jk|).
+// Every partial sum is kept per thread in a fixed order and reduced in a
+// fixed order: results are deterministic.
 #include "gst_common.cuh"
 
 namespace gst {
@@ -104,6 +108,54 @@ __global__ void __launch_bounds__(kThreadsK)
     }
 }
 
+// out_k = sum_j u_j A_jk for a row-major K x n matrix A: thread (g, c) of a
+// CTA sums the rows j = g (mod GROUPS) of column k0 + c (COLS contiguous
+// doubles per warp and row, four loads in flight), then the GROUPS partial
+// sums are added in group order.  Used twice: u = M^T c (A = M, many row
+// groups for the few columns) and f = V^T u (A = V).
+template <int COLS, int GROUPS>
+__global__ void __launch_bounds__(COLS * GROUPS)
+    krige_colsum_kernel(int64_t K, int64_t n, const double *__restrict__ u,
+                        const double *__restrict__ a, double *__restrict__ out) {
+    __shared__ double part[GROUPS][COLS];
+    const int c = threadIdx.x % COLS;
+    const int g = threadIdx.x / COLS;
+    const int64_t k = blockIdx.x * static_cast<int64_t>(COLS) + c;
+    double acc = 0.0;
+    if (k < n) {
+        int64_t j = g;
+        for (; j + 3 * GROUPS < K; j += 4 * GROUPS) {
+            const double v0 = a[j * n + k];
+            const double v1 = a[(j + GROUPS) * n + k];
+            const double v2 = a[(j + 2 * GROUPS) * n + k];
+            const double v3 = a[(j + 3 * GROUPS) * n + k];
+            acc = fma(u[j], v0, acc);
+            acc = fma(u[j + GROUPS], v1, acc);
+            acc = fma(u[j + 2 * GROUPS], v2, acc);
+            acc = fma(u[j + 3 * GROUPS], v3, acc);
+        }
+        for (; j < K; j += GROUPS) acc = fma(u[j], a[j * n + k], acc);
+    }
+    part[g][c] = acc;
+    __syncthreads();
+    if (g == 0 && k < n) {
+        double f = part[0][c];
+#pragma unroll
+        for (int q = 1; q < GROUPS; ++q) f += part[q][c];
+        out[k] = f;
+    }
+}
+
+template <int COLS, int GROUPS>
+cudaError_t launch_colsum(int64_t K, int64_t n, const double *u, const double *a,
+                          double *out, cudaStream_t s) {
+    const int64_t blocks = ceil_div(n, COLS);
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    krige_colsum_kernel<COLS, GROUPS>
+        <<<static_cast<unsigned>(blocks), COLS * GROUPS, 0, s>>>(K, n, u, a, out);
+    return cudaGetLastError();
+}
+
 }  // namespace
 }  // namespace gst
 
@@ -125,6 +177,16 @@ int gst_calc_field_krige(int64_t n_cond, int64_t n_pts, const double *krig_mat,
     }
     if (krig_mat == nullptr || krig_vecs == nullptr || cond == nullptr)
         return GST_ERR_INVALID_ARGUMENT;
+    if (error == nullptr) {
+        // field only: u = M^T c, then f = V^T u
+        if (gst::ceil_div(n_pts, 64) > 0x7fffffffLL) return GST_ERR_TOO_LARGE;
+        gst::StreamScratch u;
+        GST_TRY_CUDA(u.alloc(sizeof(double) * n_cond, s));
+        double *du = static_cast<double *>(u.ptr);
+        GST_TRY_CUDA((gst::launch_colsum<32, 32>(n_cond, n_cond, cond, krig_mat, du, s)));
+        GST_TRY_CUDA((gst::launch_colsum<64, 4>(n_cond, n_pts, du, krig_vecs, field, s)));
+        return GST_OK;
+    }
     const int64_t blocks = gst::ceil_div(n_pts, gst::kKT);
     if (blocks > 0x7fffffffLL) return GST_ERR_TOO_LARGE;
     gst::krige_kernel<<<static_cast<unsigned>(blocks), gst::kThreadsK, 0, s>>>(

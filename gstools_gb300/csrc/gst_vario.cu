@@ -221,6 +221,342 @@ __global__ void __launch_bounds__(kVarioThreads)
     }
 }
 
+// ------------------------------------------------ omnidirectional, fast path --
+//
+// Euclidean omnidirectional estimator with at most kOmniMaxBins bins.  The
+// squared distance is formed in FP32 from hi + lo splits of the coordinates
+// (x = hi + lo + r, |r| <= 2^-48 |x|).  Each difference is then off by at
+// most 2^-23 |dx| + 2^-46 X (X the largest |coordinate| of the tile), and
+// the squared distance, against the reference's FP64 value, by at most
+//     B = 2^-21 d2 + 2^-44 X sqrt(d2) + 2^-90 X^2
+// (checked on 3000 random point clouds, offsets 1e-6 .. 1e12, close and far
+// pairs: largest error 0.72 B).  A pair whose FP32 value lies within
+//     G_i = 2^-19 e_i^2 + 2^-41 X e_i + 2^-88 X^2
+// (at least four times B at d2 = e_i^2) of a squared edge is binned from the
+// exact FP64 distance instead, so every pair lands in the reference's bin.  Each thread
+// adds its pairs' FP64 terms into a private histogram in shared memory (no
+// atomics; bin-major, thread-minor: conflict-free for distinct bins); the
+// CTAs are persistent over the upper-triangle tiles and flush their
+// histograms (fixed-order sum over the threads, one global atomic per bin)
+// once at the end, or sooner if a 32-bit count could overflow.
+constexpr int kOmniThreads = 128;
+constexpr int kOmniMaxBins = 64;
+constexpr int kOmniTab = 1024;   // cells of the squared-distance bin table
+constexpr float kGuardRel = 1.9073486328125e-06f;     // 2^-19
+constexpr float kGuardAbs = 4.547473508864641e-13f;   // 2^-41
+constexpr float kGuardSq = 3.2311742677852644e-27f;   // 2^-88
+
+struct OmniArgs {
+    int64_t n;
+    int64_t f_max;
+    const double *f;      // f_max x n
+    const double *pos;    // dim x n
+    int n_bins;
+    const double *edges;  // n_bins + 1
+    int est;
+    int64_t n_tiles;      // 128-point tiles per axis
+    int64_t n_tri;        // upper-triangle tiles
+    double *sums;
+    unsigned long long *counts;
+};
+
+__host__ __device__ constexpr size_t omni_smem_bytes(int nb) {
+    return sizeof(double) * (nb + 1)                        // edges
+           + sizeof(float) * 2 * (nb + 1)                   // squared edges, guards
+           + sizeof(float4) * kOmniThreads * 2              // k-tile hi/lo, |x| max
+           + sizeof(double) * kOmniThreads                  // k-tile field 0
+           + sizeof(float) * 4                              // tile |x| max per warp
+           + sizeof(double) * kOmniThreads                  // field 0 at j, per lane
+           + sizeof(unsigned int) * 2 * kOmniThreads        // per-warp queues (64)
+           + kOmniTab                                       // bin table
+           + (sizeof(double) + sizeof(unsigned int)) * nb * kOmniThreads;
+}
+
+__device__ __forceinline__ void tile_of(int64_t t, int64_t &jt, int64_t &kt) {
+    int64_t r = static_cast<int64_t>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) / 2.0);
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;
+    while (r * (r + 1) / 2 > t) --r;
+    jt = t - r * (r + 1) / 2;   // 0..r
+    kt = r;
+}
+
+template <int DIM>
+__device__ __forceinline__ double exact_d2(double p0, double p1, double p2,
+                                           const double *pos, int64_t n, int64_t k) {
+    double dd = p0 - pos[k];
+    double d2 = __dadd_rn(0.0, __dmul_rn(dd, dd));
+    if (DIM > 1) {
+        dd = p1 - pos[n + k];
+        d2 = __dadd_rn(d2, __dmul_rn(dd, dd));
+    }
+    if (DIM > 2) {
+        dd = p2 - pos[2 * n + k];
+        d2 = __dadd_rn(d2, __dmul_rn(dd, dd));
+    }
+    return d2;
+}
+
+// Bin of pair (j, k) or -1: FP32 squared distance against the squared
+// edges, the exact FP64 distance within the guard of an edge (or for every
+// pair of a tile whose coordinates are out of the FP32 bound's range).
+template <int DIM>
+__device__ __forceinline__ int pair_bin(int kl, const float *jh, const float *jl,
+                                        const double *pj, const float4 *k_hi,
+                                        const float4 *k_lo, const float *e2f,
+                                        const float *guard, const double *edges, int nb,
+                                        float lim, const signed char *tab, float tscale,
+                                        bool exact_only, const double *pos, int64_t n,
+                                        int64_t k) {
+    bool exact = exact_only;
+    int bin = -1;
+    if (!exact) {
+        const float4 kh = k_hi[kl], klo = k_lo[kl];
+        const float dx = (jh[0] - kh.x) + (jl[0] - klo.x);
+        float f2 = dx * dx;
+        if (DIM > 1) {
+            const float dy = (jh[1] - kh.y) + (jl[1] - klo.y);
+            f2 = fmaf(dy, dy, f2);
+        }
+        if (DIM > 2) {
+            const float dz = (jh[2] - kh.z) + (jl[2] - klo.z);
+            f2 = fmaf(dz, dz, f2);
+        }
+        if (!(f2 <= lim)) return -1;   // beyond the last edge (or NaN)
+        // last lo with e2f[lo] <= f2: table guess, then exact steps
+        int lo = tab[min(__float2int_rz(f2 * tscale), kOmniTab - 1)];
+        while (lo >= 0 && e2f[lo] > f2) --lo;
+        while (lo < nb && e2f[lo + 1] <= f2) ++lo;
+        exact = (lo >= 0 && fabsf(f2 - e2f[lo]) <= guard[lo]) ||
+                (lo + 1 <= nb && fabsf(f2 - e2f[lo + 1]) <= guard[lo + 1]);
+        bin = (lo >= 0 && lo < nb) ? lo : -1;
+    }
+    if (exact) {
+        const double d2 = exact_d2<DIM>(pj[0], pj[1], pj[2], pos, n, k);
+        if (!(d2 >= 0.0)) return -1;
+        const double dist = sqrt(d2);
+        int lo = -1, hi = nb + 1;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (edges[mid] <= dist) lo = mid; else hi = mid;
+        }
+        bin = (lo >= 0 && lo < nb) ? lo : -1;
+    }
+    return bin;
+}
+
+template <bool CRESSIE>
+__device__ __forceinline__ double estimate_t(double d) {
+    return CRESSIE ? sqrt(fabs(d)) : d * d;
+}
+
+template <int DIM, bool CRESSIE>
+__global__ void __launch_bounds__(kOmniThreads)
+    vario_omni_kernel(const OmniArgs a) {
+    extern __shared__ __align__(16) double sh[];
+    const int nb = a.n_bins;
+    const int tid = threadIdx.x;
+    double *edges = sh;
+    float *e2f = reinterpret_cast<float *>(edges + (nb + 1));
+    float *guard = e2f + (nb + 1);
+    // 16-byte aligned region after the edge tables
+    const size_t off = (sizeof(double) * (nb + 1) + sizeof(float) * 2 * (nb + 1) + 15) / 16 * 16;
+    float4 *k_hi = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(sh) + off);
+    float4 *k_lo = k_hi + kOmniThreads;
+    double *k_f = reinterpret_cast<double *>(k_lo + kOmniThreads);
+    float *w_max = reinterpret_cast<float *>(k_f + kOmniThreads);
+    double *w_fj = reinterpret_cast<double *>(w_max + 4);
+    unsigned int *w_queue = reinterpret_cast<unsigned int *>(w_fj + kOmniThreads);
+    double *h_sum = reinterpret_cast<double *>(w_queue + 2 * kOmniThreads);
+    unsigned int *h_cnt = reinterpret_cast<unsigned int *>(h_sum + nb * kOmniThreads);
+    signed char *tab = reinterpret_cast<signed char *>(h_cnt + nb * kOmniThreads);
+
+    for (int i = tid; i <= nb; i += kOmniThreads) {
+        const double e = a.edges[i];
+        edges[i] = e;
+        e2f[i] = e > 0.0 ? __double2float_rn(e * e) : -1.0f;
+    }
+    for (int i = tid; i < nb * kOmniThreads; i += kOmniThreads) {
+        h_sum[i] = 0.0;
+        h_cnt[i] = 0u;
+    }
+    __syncthreads();
+    // tab[c]: last bin lo with e2f[lo] <= c / tscale (cell c of [0, e2f[nb]])
+    const float tscale = e2f[nb] > 0.0f ? static_cast<float>(kOmniTab) / e2f[nb] : 0.0f;
+    for (int c = tid; c < kOmniTab; c += kOmniThreads) {
+        const float v = tscale > 0.0f ? static_cast<float>(c) / tscale : 0.0f;
+        int lo = -1, hi = nb + 1;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (e2f[mid] <= v) lo = mid; else hi = mid;
+        }
+        tab[c] = static_cast<signed char>(lo > nb ? nb : lo);
+    }
+    // tiles between flushes such that no 32-bit count overflows
+    // a lane adds at most kOmniThreads + 1 terms per field and tile (its own
+    // pairs, or one queue entry per round of 32)
+    const int64_t per_tile = static_cast<int64_t>(kOmniThreads + 1) * (a.f_max > 1 ? a.f_max : 1);
+    const int64_t flush_every = per_tile >= 0xffffffffLL ? 1 : 0xffffffffLL / per_tile;
+    int64_t since_flush = 0;
+
+    auto flush = [&]() {
+        __syncthreads();
+        for (int b = tid; b < nb; b += kOmniThreads) {
+            double g = 0.0;
+            unsigned long long c = 0ull;
+            for (int t = 0; t < kOmniThreads; ++t) {
+                g += h_sum[b * kOmniThreads + t];
+                c += h_cnt[b * kOmniThreads + t];
+                h_sum[b * kOmniThreads + t] = 0.0;
+                h_cnt[b * kOmniThreads + t] = 0u;
+            }
+            if (c != 0ull) {
+                atomicAdd(&a.sums[b], g);
+                atomicAdd(&a.counts[b], c);
+            }
+        }
+        __syncthreads();
+    };
+
+    for (int64_t t = blockIdx.x; t < a.n_tri; t += gridDim.x) {
+        int64_t jt, kt;
+        tile_of(t, jt, kt);
+        const int64_t j = jt * kOmniThreads + tid;
+        const int64_t kstage = kt * kOmniThreads + tid;
+        __syncthreads();   // the previous tile's readers are done
+        float xmax = 0.0f;
+        {
+            float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+            if (kstage < a.n) {
+                float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const double x = a.pos[d * a.n + kstage];
+                    h[d] = __double2float_rn(x);
+                    l[d] = __double2float_rn(x - static_cast<double>(h[d]));
+                    xmax = fmaxf(xmax, fabsf(h[d]));
+                }
+                // w: 1 when field 0 of this point is a number
+                const double fk = a.f_max > 0 ? a.f[kstage] : 0.0;
+                hi = make_float4(h[0], h[1], h[2],
+                                 (a.f_max > 0 && !isnan(fk)) ? 1.f : 0.f);
+                lo = make_float4(l[0], l[1], l[2], 0.f);
+                k_f[tid] = fk;
+            }
+            k_hi[tid] = hi;
+            k_lo[tid] = lo;
+        }
+        double pj[3] = {0.0, 0.0, 0.0};
+        float jh[3] = {0.f, 0.f, 0.f}, jl[3] = {0.f, 0.f, 0.f};
+        if (j < a.n) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                pj[d] = a.pos[d * a.n + j];
+                jh[d] = __double2float_rn(pj[d]);
+                jl[d] = __double2float_rn(pj[d] - static_cast<double>(jh[d]));
+                xmax = fmaxf(xmax, fabsf(jh[d]));
+            }
+        }
+        // tile maximum of |x| (NaN propagates as "not finite" below)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            xmax = fmaxf(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
+        if ((tid & 31) == 0) w_max[tid >> 5] = xmax;
+        __syncthreads();
+        const float X = fmaxf(fmaxf(w_max[0], w_max[1]), fmaxf(w_max[2], w_max[3]));
+        // the FP32 bound holds for moderate coordinates; otherwise every
+        // pair of the tile takes the exact FP64 distance
+        const bool exact_only = !(X >= 1e-18f && X <= 1e18f);
+        for (int i = tid; i <= nb; i += kOmniThreads) {
+            const float e = __double2float_rn(fabs(edges[i]));
+            guard[i] = edges[i] > 0.0
+                           ? kGuardRel * e2f[i] + kGuardAbs * X * e + kGuardSq * X * X
+                           : 0.0f;
+        }
+        __syncthreads();
+        const float lim = e2f[nb] + guard[nb];
+        const int64_t rest = a.n - kt * kOmniThreads;
+        const int kl1 = rest < kOmniThreads ? static_cast<int>(rest) : kOmniThreads;
+        const double fj = (j < a.n && a.f_max > 0) ? a.f[j] : 0.0;
+        if (a.f_max == 1) {
+            // One field: the lanes run the same k sequence, and the pairs
+            // that fall in a bin (about 40 % of them) are queued per warp, so
+            // the FP64 terms run on full warps.  Queue entry: bin << 16 |
+            // k << 5 | lane of j.
+            const int lane = tid & 31, warp = tid >> 5;
+            unsigned int *q = w_queue + warp * 64;
+            w_fj[tid] = fj;
+            const bool row_ok = j < a.n && !isnan(fj);
+            const int kl_first = (jt == kt) ? warp * 32 + 1 : 0;
+            int qn = 0;
+            if (__any_sync(0xffffffffu, row_ok)) {
+                for (int kl = kl_first; kl < kl1; ++kl) {
+                    int bin = -1;
+                    if (row_ok && (jt != kt || kl > tid) && k_hi[kl].w != 0.f)
+                        bin = pair_bin<DIM>(kl, jh, jl, pj, k_hi, k_lo, e2f, guard, edges,
+                                            nb, lim, tab, tscale, exact_only, a.pos, a.n,
+                                            kt * kOmniThreads + kl);
+                    const unsigned int m = __ballot_sync(0xffffffffu, bin >= 0);
+                    if (bin >= 0)
+                        q[qn + __popc(m & ((1u << lane) - 1u))] =
+                            (static_cast<unsigned int>(bin) << 16) |
+                            (static_cast<unsigned int>(kl) << 5) | lane;
+                    qn += __popc(m);
+                    if (qn >= 32) {
+                        __syncwarp();
+                        const unsigned int e = q[lane];
+                        const double d = k_f[(e >> 5) & 127u] - w_fj[warp * 32 + (e & 31u)];
+                        h_sum[(e >> 16) * kOmniThreads + tid] += estimate_t<CRESSIE>(d);
+                        h_cnt[(e >> 16) * kOmniThreads + tid] += 1u;
+                        __syncwarp();
+                        if (lane < qn - 32) q[lane] = q[32 + lane];
+                        __syncwarp();
+                        qn -= 32;
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane < qn) {
+                const unsigned int e = q[lane];
+                const double d = k_f[(e >> 5) & 127u] - w_fj[warp * 32 + (e & 31u)];
+                h_sum[(e >> 16) * kOmniThreads + tid] += estimate_t<CRESSIE>(d);
+                h_cnt[(e >> 16) * kOmniThreads + tid] += 1u;
+            }
+        } else if (j < a.n) {
+            // no field or several fields: per-lane terms
+            const bool fj_ok = a.f_max > 0 && !isnan(fj);
+            const int kl0 = (jt == kt) ? tid + 1 : 0;
+            for (int kl = kl0; kl < kl1; ++kl) {
+                const int64_t k = kt * kOmniThreads + kl;
+                const int bin = pair_bin<DIM>(kl, jh, jl, pj, k_hi, k_lo, e2f, guard, edges,
+                                              nb, lim, tab, tscale, exact_only, a.pos,
+                                              a.n, k);
+                if (bin < 0) continue;
+                double g = 0.0;
+                unsigned int c = 0u;
+                if (fj_ok && k_hi[kl].w != 0.f) {
+                    g = estimate_t<CRESSIE>(k_f[kl] - fj);
+                    c = 1u;
+                }
+                for (int64_t m = 1; m < a.f_max; ++m) {
+                    const double fa = a.f[m * a.n + k], fb = a.f[m * a.n + j];
+                    if (isnan(fa) || isnan(fb)) continue;
+                    g += estimate_t<CRESSIE>(fa - fb);
+                    ++c;
+                }
+                if (c != 0u) {
+                    h_sum[bin * kOmniThreads + tid] += g;
+                    h_cnt[bin * kOmniThreads + tid] += c;
+                }
+            }
+        }
+        if (++since_flush >= flush_every) {
+            flush();
+            since_flush = 0;
+        }
+    }
+    flush();
+}
+
 __device__ __forceinline__ double normalise(int est, double g, unsigned long long c) {
     const double cnt = c > 1ull ? static_cast<double>(c) : 1.0;
     if (est == 'c') {
@@ -292,6 +628,29 @@ __global__ void vario_structured_finish(int64_t n0, int64_t n_chunks, int est,
     vario[k] = normalise(est, g, c);
 }
 
+template <int DIM, bool CRESSIE>
+cudaError_t launch_omni_t(const OmniArgs &o, cudaStream_t s) {
+    const size_t smem = omni_smem_bytes(o.n_bins) + 16;
+    cudaError_t e = cudaFuncSetAttribute(vario_omni_kernel<DIM, CRESSIE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, vario_omni_kernel<DIM, CRESSIE>, kOmniThreads, smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = std::min<int64_t>(
+        o.n_tri, static_cast<int64_t>(std::max(per_sm, 1)) * sm_count());
+    vario_omni_kernel<DIM, CRESSIE>
+        <<<static_cast<unsigned>(grid), kOmniThreads, smem, s>>>(o);
+    return cudaGetLastError();
+}
+
+template <int DIM>
+cudaError_t launch_omni(const OmniArgs &o, cudaStream_t s) {
+    return o.est == 'c' ? launch_omni_t<DIM, true>(o, s) : launch_omni_t<DIM, false>(o, s);
+}
+
 int pairs_impl(const VarioArgs &args, double *vario, int64_t *counts, cudaStream_t s) {
     const int nh = (args.d_max > 0 ? args.d_max : 1) * args.n_bins;
     VarioArgs a = args;
@@ -299,6 +658,30 @@ int pairs_impl(const VarioArgs &args, double *vario, int64_t *counts, cudaStream
     a.counts = reinterpret_cast<unsigned long long *>(counts);
     GST_TRY_CUDA(cudaMemsetAsync(a.sums, 0, sizeof(double) * nh, s));
     GST_TRY_CUDA(cudaMemsetAsync(a.counts, 0, sizeof(unsigned long long) * nh, s));
+    if (a.d_max == 0 && !a.haversine && a.n_bins <= kOmniMaxBins) {
+        OmniArgs o{};
+        o.n = a.n;
+        o.f_max = a.f_max;
+        o.f = a.f;
+        o.pos = a.pos;
+        o.n_bins = a.n_bins;
+        o.edges = a.edges;
+        o.est = a.est;
+        o.n_tiles = ceil_div(a.n, kOmniThreads);
+        o.n_tri = o.n_tiles * (o.n_tiles + 1) / 2;
+        o.sums = a.sums;
+        o.counts = a.counts;
+        if (o.n_tri > 0) {
+            cudaError_t e = a.dim == 1   ? launch_omni<1>(o, s)
+                            : a.dim == 2 ? launch_omni<2>(o, s)
+                                         : launch_omni<3>(o, s);
+            GST_TRY_CUDA(e);
+        }
+        vario_normalise_kernel<<<static_cast<unsigned>(ceil_div(nh, 256)), 256, 0, s>>>(
+            a.est, nh, a.sums, a.counts);
+        GST_TRY_CUDA(cudaGetLastError());
+        return GST_OK;
+    }
     const int64_t n_tiles = ceil_div(args.n, kPairTile);
     const int64_t blocks = n_tiles * (n_tiles + 1) / 2;
     if (blocks > 0x7fffffffLL) return GST_ERR_TOO_LARGE;

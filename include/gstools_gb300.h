@@ -335,7 +335,9 @@ int gst_philox4x64_fill(uint64_t key0, uint64_t key1, int64_t n_blocks,
 /* (n_cond x n_cond, row-major), the right-hand sides krig_vecs (n_cond x   */
 /* n_pts, row-major) and the condition values cond (n_cond):                */
 /*   field[k] = sum_i cond[i] (M v_k)_i,  error[k] = sum_i v_ik (M v_k)_i    */
-/* (error may be NULL for the field only).  Device pointers; FP64;          */
+/* error may be NULL for the field only, computed as field = V^T (M^T c):   */
+/* n_cond^2 + n_cond n_pts flops instead of n_cond^2 n_pts, same FP64 error */
+/* bound, n_cond doubles of stream-ordered scratch.  Device pointers; FP64; */
 /* deterministic.                                                           */
 /* ----------------------------------------------------------------------- */
 int gst_calc_field_krige(int64_t n_cond, int64_t n_pts, const double *krig_mat,

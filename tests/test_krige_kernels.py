@@ -8,7 +8,8 @@ conditions, to 2 places).
 CPU: the C oracle against the numpy witness; the hook routes the reference's
 kriging wrappers (src/gstools/krige/base.py:42-60) and restores them, and
 raises without a GPU.
-GPU: field and error variance against the oracle, scale-aware FP64 bar:
+GPU: field and error variance against the oracle (and the field alone,
+computed as V^T (M^T c)), scale-aware FP64 bar:
 |diff| <= 1e-12 * sum_i (|c_i| + |v_i|) (|M| |v|)_i per point (a different
 summation order than the oracle's; rounding scales with the magnitude of the
 terms of both nested sums, not with the result, which cancels for the
@@ -87,7 +88,7 @@ def test_kernel_matches_reference_fixtures(cuda_lib, ref_goldens):
         assert _within(f, c["field"], scale), name
         assert _within(e, c["error"], scale), name
         f_only = gg.calc_field_krige(c["mat"], c["vecs"], c["cond"])
-        np.testing.assert_array_equal(f_only, f)
+        assert _within(f_only, c["field"], scale), name
 
 
 @pytest.mark.gpu
@@ -103,6 +104,8 @@ def test_kernel_matches_oracle_random(cuda_lib, k, n):
     fo, eo = oracle.c_krige(mat, vecs, cond)
     _, _, scale = oracle.np_krige(mat, vecs, cond)
     assert _within(f, fo, scale) and _within(e, eo, scale)
+    # field only: V^T (M^T c), another summation order under the same bar
+    assert _within(gg.calc_field_krige(mat, vecs, cond), fo, scale)
 
 
 @pytest.mark.gpu

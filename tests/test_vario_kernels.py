@@ -193,6 +193,38 @@ def test_gpu_unstructured_random(cuda_lib, dim, n, f_max, est):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("case", ["offset", "close_far_out", "bins64", "bins65"])
+def test_gpu_unstructured_fp32_distance_guard(cuda_lib, case):
+    """The FP32 squared distance and its guard: integer coordinates far from
+    the origin (every pair distance that is an integer hits an integer edge
+    exactly), tiny distances between points at 3e8 (the quadratic guard
+    term), and the 64-bin limit of the private-histogram kernel and one bin
+    past it (shared-atomic kernel).  Counts exact, sums within 1e-12."""
+    import gstools_gb300.variogram as gv
+
+    rng = np.random.RandomState(77)
+    n = 1500
+    if case == "offset":
+        pos = 1.0e6 + np.round(rng.uniform(0, 40, size=(2, n)))
+        edges = np.arange(0.0, 31.0)
+    elif case == "close_far_out":
+        base = 3.0e8 + rng.uniform(0, 1, size=(3, 1))
+        pos = base + np.round(rng.uniform(-5, 5, size=(3, n))) * 2.0 ** -22
+        edges = np.arange(0.0, 12.0) * 2.0 ** -22
+    else:
+        nb = 64 if case == "bins64" else 65
+        pos = rng.uniform(0, 100, size=(3, n))
+        pos[:, : n // 2] = np.round(pos[:, : n // 2])
+        edges = np.linspace(0.0, 100.0, nb + 1)
+    f = rng.normal(size=(1, n))
+    g, c = gv.unstructured(f, edges, pos, "m")
+    go, co = oracle.c_vario_unstructured(f, edges, pos, "m")
+    assert co.sum() > 0
+    np.testing.assert_array_equal(c, co)
+    np.testing.assert_allclose(g, go, rtol=REL, atol=0)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("separate", [False, True])
 def test_gpu_directional_random(cuda_lib, separate):
     import gstools_gb300.variogram as gv
