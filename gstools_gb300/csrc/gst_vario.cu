@@ -15,12 +15,16 @@
 // bandwidth; separate_dirs stops at the first matching direction), for every
 // field whose two values are not NaN.  Their loop runs the bins outermost
 // and so evaluates every pair once per bin; here every pair is evaluated
-// once: CTAs own 128 x 128 tiles of the upper triangle of the pair matrix,
-// bin by binary search over the squared edges (the exact square root is
-// taken only when the squared distance is within a few ulps of a squared
-// edge, so bins match the reference's sqrt-then-compare), and add into
-// shared-memory histograms flushed with atomics.  Sums of positive terms in
-// a different order: equal to the reference within rounding; counts exact.
+// once, over 128 x 128 tiles of the upper triangle of the pair matrix.
+// Euclidean omnidirectional estimates with up to 64 bins take the fast path
+// (vario_omni_kernel): FP32 squared distances from hi + lo coordinate splits
+// with a proven error bound, a bin table, the exact FP64 distance only near
+// an edge, per-thread histograms, and for one field the binned pairs queued
+// per warp so the FP64 terms run on full warps.  Directional, haversine and
+// many-bin estimates use vario_pairs_kernel (FP64 distances, FP32 binning
+// with the same exact fallback, shared-memory histograms).  Sums of positive
+// terms in a different order: equal to the reference within rounding;
+// counts exact.
 // The structured estimator runs one CTA per (lag, column chunk), partial
 // sums reduced in a fixed order (deterministic).
 #include <algorithm>
@@ -488,30 +492,41 @@ __global__ void __launch_bounds__(kOmniThreads)
             const bool row_ok = j < a.n && !isnan(fj);
             const int kl_first = (jt == kt) ? warp * 32 + 1 : 0;
             int qn = 0;
+            // queue the pair (bin >= 0) and run the FP64 terms of a full round
+            auto enqueue = [&](int bin, int kl) {
+                const unsigned int m = __ballot_sync(0xffffffffu, bin >= 0);
+                if (bin >= 0)
+                    q[qn + __popc(m & ((1u << lane) - 1u))] =
+                        (static_cast<unsigned int>(bin) << 16) |
+                        (static_cast<unsigned int>(kl) << 5) | lane;
+                qn += __popc(m);
+                if (qn >= 32) {
+                    __syncwarp();
+                    const unsigned int e = q[lane];
+                    const double d = k_f[(e >> 5) & 127u] - w_fj[warp * 32 + (e & 31u)];
+                    h_sum[(e >> 16) * kOmniThreads + tid] += estimate_t<CRESSIE>(d);
+                    h_cnt[(e >> 16) * kOmniThreads + tid] += 1u;
+                    __syncwarp();
+                    if (lane < qn - 32) q[lane] = q[32 + lane];
+                    __syncwarp();
+                    qn -= 32;
+                }
+            };
+            auto bin_of = [&](int kl) {
+                if (kl < kl1 && row_ok && (jt != kt || kl > tid) && k_hi[kl].w != 0.f)
+                    return pair_bin<DIM>(kl, jh, jl, pj, k_hi, k_lo, e2f, guard, edges, nb,
+                                         lim, tab, tscale, exact_only, a.pos, a.n,
+                                         kt * kOmniThreads + kl);
+                return -1;
+            };
             if (__any_sync(0xffffffffu, row_ok)) {
-                for (int kl = kl_first; kl < kl1; ++kl) {
-                    int bin = -1;
-                    if (row_ok && (jt != kt || kl > tid) && k_hi[kl].w != 0.f)
-                        bin = pair_bin<DIM>(kl, jh, jl, pj, k_hi, k_lo, e2f, guard, edges,
-                                            nb, lim, tab, tscale, exact_only, a.pos, a.n,
-                                            kt * kOmniThreads + kl);
-                    const unsigned int m = __ballot_sync(0xffffffffu, bin >= 0);
-                    if (bin >= 0)
-                        q[qn + __popc(m & ((1u << lane) - 1u))] =
-                            (static_cast<unsigned int>(bin) << 16) |
-                            (static_cast<unsigned int>(kl) << 5) | lane;
-                    qn += __popc(m);
-                    if (qn >= 32) {
-                        __syncwarp();
-                        const unsigned int e = q[lane];
-                        const double d = k_f[(e >> 5) & 127u] - w_fj[warp * 32 + (e & 31u)];
-                        h_sum[(e >> 16) * kOmniThreads + tid] += estimate_t<CRESSIE>(d);
-                        h_cnt[(e >> 16) * kOmniThreads + tid] += 1u;
-                        __syncwarp();
-                        if (lane < qn - 32) q[lane] = q[32 + lane];
-                        __syncwarp();
-                        qn -= 32;
-                    }
+                // two independent pairs per step for latency hiding (four
+                // measured no faster)
+                for (int kl = kl_first; kl < kl1; kl += 2) {
+                    const int b0 = bin_of(kl);
+                    const int b1 = bin_of(kl + 1);
+                    enqueue(b0, kl);
+                    enqueue(b1, kl + 1);
                 }
             }
             __syncwarp();
