@@ -225,6 +225,25 @@ def test_gpu_unstructured_fp32_distance_guard(cuda_lib, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(512, 33), (513, 7), (2, 1), (300, 64)])
+def test_gpu_structured_tiled_limits(cuda_lib, shape):
+    """Axis variogram at the tiled kernel's row limit (512 rows in shared
+    memory), one row past it (per-lag kernel), a single lag, and whole
+    32-column blocks; with and without a mask, both estimators."""
+    import gstools_gb300.variogram as gv
+
+    rng = np.random.RandomState(shape[0])
+    fld = rng.normal(size=shape) + 3.0
+    mask = rng.uniform(size=shape) < 0.2
+    for est in ("m", "c"):
+        np.testing.assert_allclose(gv.structured(fld, est),
+                                   oracle.c_vario_structured(fld, est), rtol=REL)
+        np.testing.assert_allclose(gv.ma_structured(fld, mask, est),
+                                   oracle.c_vario_structured(fld, est, mask=mask),
+                                   rtol=REL)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("separate", [False, True])
 def test_gpu_directional_random(cuda_lib, separate):
     import gstools_gb300.variogram as gv
