@@ -624,6 +624,60 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Structured, tiled: one CTA per block of 32 columns, the whole block
+// (n0 <= kTiledMaxRows rows) in shared memory.  Warp g handles the lags
+// k = g + 1, g + 9, ...; lane c one column: per lag it sums the pairs
+// (i, i + k) of its column in row order, the warp adds its 32 column sums
+// in a fixed order (shuffle tree) and lane 0 writes the CTA's partial for k.
+// Per pair two shared loads, one DADD and one DFMA: the FP64 pipe bounds it.
+constexpr int kTiledCols = 32;
+constexpr int kTiledWarps = 8;
+constexpr int kTiledMaxRows = 512;
+
+template <bool CRESSIE, bool MASKED>
+__global__ void __launch_bounds__(kTiledCols * kTiledWarps)
+    vario_structured_tiled_kernel(int64_t n0, int64_t rest, const double *__restrict__ f,
+                                  const unsigned char *__restrict__ mask, int64_t n_chunks,
+                                  double *__restrict__ part_sum,
+                                  unsigned long long *__restrict__ part_cnt) {
+    extern __shared__ __align__(16) double fs[];   // [n0][32], then mask bytes
+    unsigned char *ms = reinterpret_cast<unsigned char *>(fs + n0 * kTiledCols);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t chunk = blockIdx.x;
+    const int64_t col = chunk * kTiledCols + lane;
+    const bool col_ok = col < rest;
+    for (int64_t i = warp; i < n0; i += kTiledWarps) {
+        fs[i * kTiledCols + lane] = col_ok ? f[i * rest + col] : 0.0;
+        if (MASKED) ms[i * kTiledCols + lane] = col_ok ? mask[i * rest + col] : 1;
+    }
+    __syncthreads();
+    for (int64_t k = warp + 1; k < n0; k += kTiledWarps) {
+        double acc = 0.0;
+        unsigned int cnt = 0u;
+        if (col_ok) {
+            for (int64_t i = 0; i + k < n0; ++i) {
+                const double d = fs[i * kTiledCols + lane] - fs[(i + k) * kTiledCols + lane];
+                if (MASKED) {
+                    if (ms[i * kTiledCols + lane] | ms[(i + k) * kTiledCols + lane]) continue;
+                    ++cnt;
+                }
+                if (CRESSIE) acc += sqrt(fabs(d));
+                else acc = fma(d, d, acc);
+            }
+            if (!MASKED) cnt = static_cast<unsigned int>(n0 - k);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_down_sync(0xffffffffu, acc, o);
+            cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+        }
+        if (lane == 0) {
+            part_sum[(k - 1) * n_chunks + chunk] = acc;
+            part_cnt[(k - 1) * n_chunks + chunk] = cnt;
+        }
+    }
+}
+
 __global__ void vario_structured_finish(int64_t n0, int64_t n_chunks, int est,
                                         const double *part_sum,
                                         const unsigned long long *part_cnt,
@@ -795,7 +849,9 @@ int gst_vario_structured(int64_t n0, int64_t rest, const double *f,
     if (vario == nullptr || (rest > 0 && f == nullptr)) return GST_ERR_INVALID_ARGUMENT;
     if (gst::current_device() < 0) return GST_ERR_NO_DEVICE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const int64_t n_chunks = std::max<int64_t>(1, gst::ceil_div(rest, 256));
+    const bool tiled = n0 <= gst::kTiledMaxRows;
+    const int64_t n_chunks =
+        std::max<int64_t>(1, gst::ceil_div(rest, tiled ? gst::kTiledCols : 256));
     const int64_t lags = n0 - 1;
     if (lags > 65535 || n_chunks > 0x7fffffffLL) return GST_ERR_TOO_LARGE;
     gst::StreamScratch scratch;
@@ -803,7 +859,25 @@ int gst_vario_structured(int64_t n0, int64_t rest, const double *f,
     GST_TRY_CUDA(scratch.alloc(parts * (sizeof(double) + sizeof(unsigned long long)), s));
     double *psum = static_cast<double *>(scratch.ptr);
     auto *pcnt = reinterpret_cast<unsigned long long *>(psum + parts);
-    if (lags > 0) {
+    if (lags > 0 && tiled) {
+        if (rest == 0) {
+            GST_TRY_CUDA(cudaMemsetAsync(psum, 0, parts * sizeof(double), s));
+            GST_TRY_CUDA(cudaMemsetAsync(pcnt, 0, parts * sizeof(unsigned long long), s));
+        } else {
+            const size_t smem = static_cast<size_t>(n0) * gst::kTiledCols *
+                                (sizeof(double) + (mask ? 1 : 0));
+            auto *kern = estimator == 'c'
+                             ? (mask ? gst::vario_structured_tiled_kernel<true, true>
+                                     : gst::vario_structured_tiled_kernel<true, false>)
+                             : (mask ? gst::vario_structured_tiled_kernel<false, true>
+                                     : gst::vario_structured_tiled_kernel<false, false>);
+            GST_TRY_CUDA(cudaFuncSetAttribute(
+                kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+            kern<<<static_cast<unsigned>(n_chunks), gst::kTiledCols * gst::kTiledWarps,
+                   smem, s>>>(n0, rest, f, mask, n_chunks, psum, pcnt);
+            GST_TRY_CUDA(cudaGetLastError());
+        }
+    } else if (lags > 0) {
         const dim3 grid(static_cast<unsigned>(n_chunks), static_cast<unsigned>(lags));
         gst::vario_structured_kernel<<<grid, 256, 0, s>>>(n0, rest, f, mask, estimator,
                                                           n_chunks, psum, pcnt);
