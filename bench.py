@@ -24,6 +24,10 @@ the FP64 kernel, with the plain FP64 kernel's throughput reported beside it.
                 reference's own kernels are in the external gstools-cython
                 package and cannot be built here), on the same config.
 
+Defaults: 200 timed steps after 3 warm-up steps (about 70 ms of timed
+work, so the 10 ms clock sampler sees the timed region); ``clocks`` reports
+the samples taken inside it.
+
 Multi-GPU (``torchrun --nproc-per-node N``): every rank runs the full
 workload on its own GPU (replicas, weak scaling), timing is the max over
 ranks.
@@ -58,7 +62,9 @@ TC_DRAM_BYTES_PER_LAUNCH = 34.6e6
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=None,
+                   help="timed steps (default 200 for the headline grid, "
+                        "10 for the other workloads)")
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--grid", type=int, default=GRID)
@@ -78,7 +84,10 @@ def parse():
                         "512 Matern realizations; incompr: 3-D incompressible "
                         "field, 192^3; adjoint: gradients of a 3-D field; "
                         "krige: ordinary kriging; vario: empirical variogram")
-    return p.parse_args()
+    args = p.parse_args()
+    if args.steps is None:
+        args.steps = 200 if args.workload == "grid" else 10
+    return args
 
 
 def load_modes():
@@ -98,7 +107,7 @@ def dist_env():
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons."""
 
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,"
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,"
               "clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,"
@@ -114,12 +123,25 @@ class Clocks:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}",
                  f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE,
+                 "-lms", "10"], stdout=subprocess.PIPE,
                 stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
 
-    def stop(self):
+    @staticmethod
+    def _stamp(text):
+        import datetime
+
+        try:
+            return datetime.datetime.strptime(
+                text, "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
+
+    def stop(self, window=None):
+        """Median SM clock and throttle reasons of the samples taken inside
+        `window` = (t0, t1) (host time.time()), or of all samples when none
+        falls inside it."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         self.proc.terminate()
@@ -128,27 +150,32 @@ class Clocks:
         except subprocess.TimeoutExpired:
             self.proc.kill()
             out, _ = self.proc.communicate()
-        sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
+        rows = []
         for line in out.strip().splitlines():
             parts = [s.strip() for s in line.split(",")]
-            if len(parts) < 8:
+            if len(parts) < 9:
                 continue
             try:
-                sm.append(float(parts[0]))
-                smax.append(float(parts[1]))
+                row = (self._stamp(parts[0]), float(parts[1]), float(parts[2]),
+                       {n for n, v in zip(names, parts[5:9])
+                        if v.lower().startswith("active")})
             except ValueError:
                 continue
-            for name, val in zip(names, parts[4:8]):
-                if val.lower().startswith("active"):
-                    reasons.add(name)
-        if not sm:
+            rows.append(row)
+        inside = [r for r in rows if window is not None and r[0] is not None
+                  and window[0] <= r[0] <= window[1]]
+        use = inside or rows
+        if not use:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        sm = [r[1] for r in use]
+        loaded = [x for x in sm if x > 0.5 * max(sm)] or sm
         return {"sm_mhz": statistics.median(loaded),
-                "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "sm_max_mhz": max(r[2] for r in use),
+                "reasons": sorted(set().union(*(r[3] for r in use))),
+                "samples": len(use), "samples_in_timed_region": len(inside),
+                "interval_ms": 10}
 
 
 def cpu_baseline(cov, z1, z2, axes, target_s=10.0):
@@ -194,8 +221,11 @@ def run_reference(args):
     oracle.build()
     vals = []
     base = None
+    # each step a bounded sample: the whole run stays near two and a half
+    # minutes whatever --steps is
+    per_step_s = float(np.clip(150.0 / (args.warmup + args.steps), 0.2, 5.0))
     for i in range(args.warmup + args.steps):
-        base = cpu_baseline(cov, z1, z2, axes, target_s=5.0)
+        base = cpu_baseline(cov, z1, z2, axes, target_s=per_step_s)
         if i >= args.warmup:
             vals.append(base["value"])
     value = statistics.median(vals)
@@ -353,6 +383,8 @@ def run_ours(args):
         launches_per_step = 2   # pack_modes_kernel + pointwise_kernel
         desc = "mixed-precision pointwise grid kernel"
 
+    window = [None, None]   # host time of the last timed region
+
     def timed(parts, steps, warmup):
         """Per step: L2 flush, then events around each part."""
         for _ in range(warmup):
@@ -362,6 +394,7 @@ def run_ours(args):
         barrier()
         per_part = [[] for _ in parts]
         totals = []
+        window[0] = time.time()
         for _ in range(steps):
             flush.fill_(1.0)
             evs = [torch.cuda.Event(enable_timing=True)
@@ -375,6 +408,7 @@ def run_ours(args):
                 per_part[i].append(evs[i].elapsed_time(evs[i + 1]) / 1e3)
             totals.append(evs[0].elapsed_time(evs[-1]) / 1e3)
         torch.cuda.synchronize()
+        window[1] = time.time()
         barrier()
         return totals, per_part
 
@@ -382,7 +416,7 @@ def run_ours(args):
     clocks = Clocks(local)
     clocks.start()
     totals, per_part = timed(parts, args.steps, args.warmup)
-    clk = clocks.stop()
+    clk = clocks.stop(tuple(window))
     t_step = max_over_ranks(statistics.mean(totals))
     value = world * work / t_step / 1e9
     t_main = max_over_ranks(statistics.mean(per_part[-1]))
