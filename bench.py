@@ -533,7 +533,8 @@ def run_ours(args):
         alg = 4.0 * work / t_main / 1e12
         mps = 32 if args.operands == "f16" else 16   # modes per pipeline stage
         n_pad = -(-N_MODES // mps) * mps
-        executed = 12.0 * n_pad * (-(-n // 256) * 256) * n * n / t_main / 1e12
+        nt = _native.grid_tile_cols(n)        # z tile width (MMA N)
+        executed = 12.0 * n_pad * (-(-n // nt) * nt) * n * n / t_main / 1e12
         op_note = ("FP16 MMAs (3xFP16 split, padded), FP16 runs at the bf16 "
                    "rate" if args.operands == "f16" else
                    "TF32 MMAs (3xTF32 split, padded), TF32 runs at half the "

@@ -71,6 +71,7 @@ SIGNATURES = {
                                              _dbl, _ptr]),
     "gst_grid_tc_workspace_size": (_c_int, [_c_int, _i64, _ptr,
                                             ctypes.POINTER(ctypes.c_size_t)]),
+    "gst_grid_tc_tile_cols": (_c_int, [_i64]),
     "gst_grid_tc_tables": (_c_int, [_c_int, _i64, _ptr, _ptr, _ptr, _ptr,
                                     _ptr, _ptr, ctypes.c_size_t, _ptr]),
     "gst_grid_tc_contract": (_c_int, [_c_int, _i64, _ptr, _ptr,
@@ -184,6 +185,11 @@ def set_tc_operands(kind):
         raise ValueError(f"unknown operand kind {kind!r}; use 'f16' or 'tf32'")
     prev = load().gst_grid_tc_set_operands(_TC_KINDS[kind])
     return {v: k for k, v in _TC_KINDS.items()}[prev]
+
+
+def grid_tile_cols(nz):
+    """z tile width (MMA N) of the tensor-core grid path for nz points."""
+    return load().gst_grid_tc_tile_cols(int(nz))
 
 
 def read_device_error(stream=0):

@@ -14,32 +14,36 @@
 // M is folded into the wave vectors by the caller (<k, M x> = <M^T k, x>).
 // A 2-D grid is the same with a dummy y axis of length 1 (Ey = 1).
 //
-// Precision: the per-axis tables come from an exact FP64 turn reduction of
+// Precision: the per-axis tables come from an exact turn reduction of
 // k x / (2 pi) and an FP32 sincospi of the reduced angle; every operand is
-// split into TF32 hi + lo and the GEMM runs as Ah Bh + Ah Bl + Al Bh
-// (3xTF32).  The tensor core's FP32 accumulation is not round-to-nearest
-// over long K (its error grows with the number of MMAs added into one large
-// running sum), so the modes are processed in chunks of 32: each chunk
-// accumulates from zero in tensor memory and is then added into FP32
-// registers of the epilogue threads.  Two accumulators alternate, so the
-// tensor cores fill one while the other is drained.
+// split into hi + lo parts of the operand format (FP16 by default, amplitudes
+// scaled by a power of two into FP16 range; TF32 selectable) and the GEMM
+// runs as Ah Bh + Ah Bl + Al Bh.  The tensor core's FP32 accumulation is not
+// round-to-nearest over long K, so the modes are processed in chunks (128
+// modes with FP16 operands, 32 with TF32): each chunk accumulates from zero
+// in tensor memory and is then added into FP32 registers of the epilogue
+// threads.  Two accumulators alternate, so the tensor cores fill one while
+// the other is drained.
 //
-// Kernel structure (one CTA per output tile of 128 (x, y) rows by 256 z
-// points, 320 threads):
-//   warp 0      bulk-copy (TMA) producer: per 8-mode stage the pre-split
-//               TF32 image of Ez for the tile's 256 z points (32 KB, already
-//               in the UMMA canonical K-major layout) and the stage's w*Ex and
-//               Ey table slices, into a 4-deep ring;
-//   warp 1      allocates 512 TMEM columns (two 128 x 256 FP32 accumulators)
-//               and issues tcgen05.mma from one thread, M=128 N=256 K=8,
-//               3 MMAs per K-step;
-//   warps 2-9   generate A = w Ex Ey (complex product, TF32 split; two
-//               threads per row) into a 4-deep ring of shared-memory slots,
-//               drain finished chunk accumulators into registers
-//               (tcgen05.ld), and store each row's 128-point z run with
-//               vector stores.
-// Every mbarrier wait is bounded (gst::mbar_wait); a timeout is recorded in
-// the device error word and the CTA still frees its tensor memory.
+// Kernel structure: a cluster of two CTAs (tcgen05 cta_group::2) per output
+// tile of 256 (x, y) rows (128 per CTA) by NT z points (NT = 128, 192 or
+// 256, picked per grid), M = 256, N = NT; 576 threads per CTA:
+//   warp 0      bulk-copy producer: per stage its CTA's half (NT / 2 points)
+//               of the pre-split Ez image (already in the UMMA canonical
+//               K-major layout) and the stage's w*Ex and Ey table slices,
+//               into a ring of >= 3 shared-memory slots;
+//   warp 1      leader CTA: allocates 512 TMEM columns (two accumulators)
+//               and issues tcgen05.mma from one lane, 3 MMAs per K-step;
+//               peer CTA: relays its generators' and drains' arrivals to the
+//               leader's barriers;
+//   warps 2-17  generate A = w Ex Ey (complex product, hi + lo split) for
+//               the CTA's 128 rows, drain finished chunk accumulators into
+//               registers (tcgen05.ld), and store the tile (float32 through
+//               shared memory as whole row runs).
+// Tiles of a last partial wave are split over their modes in two parts that
+// add into a zeroed output.  Every mbarrier wait is bounded; a timeout is
+// recorded in the device error word and the CTAs still free their tensor
+// memory.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -55,11 +59,14 @@ namespace {
 constexpr int kThreads = 576;
 constexpr int kGenThreads = 512;      // warps 2-17
 constexpr int kCtaRows = 128;         // (x, y) rows held by each CTA
-constexpr int kTileCols = 256;        // z points per pair tile (MMA N)
-constexpr int kCtaCols = 128;         // z rows of B held by each CTA
-constexpr int kBlockBytes = 128 * 32;  // 128 rows x 32 bytes of K (one K-step)
-constexpr uint32_t kTmemCols = 512;  // two 256-column accumulators
-constexpr int kColsPerThread = 64;   // epilogue: a quarter row of 256 columns
+constexpr int kBlockBytes = 128 * 32;  // A: 128 rows x 32 bytes of K (one K-step)
+constexpr uint32_t kTmemCols = 512;  // two accumulators of up to 256 columns
+
+// z points per pair tile (the MMA's N): 256, 192 or 128, picked per grid so
+// that the padded z extent is smallest (ties to the wider tile).  Each CTA of
+// a pair holds NT / 2 rows of B; each generator warp drains and stores a
+// quarter (NT / 4 columns) of its accumulator rows.
+__host__ __device__ constexpr int b_block_bytes(int nt) { return nt / 2 * 32; }
 
 // Operand kinds of the split GEMM.  Both carry 10 explicit mantissa bits, so
 // the three-product split (hi*hi + hi*lo + lo*hi) has the same precision;
@@ -121,18 +128,16 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
     return d;                                                    // swizzle 0
 }
 
-// Instruction descriptors, D = F32, A and B K-major, M = 256 (a CTA pair),
-// N = 256: kind::tf32 with A = B = TF32, kind::f16 with A = B = F16.
-constexpr uint32_t kIdescTf32 = (1u << 4)            // D format F32
-                                | (2u << 7)          // A format TF32
-                                | (2u << 10)         // B format TF32
-                                | ((256u >> 3) << 17)  // N
-                                | ((256u >> 4) << 24); // M
-constexpr uint32_t kIdescF16 = (1u << 4)             // D format F32
-                               | (0u << 7)           // A format F16
-                               | (0u << 10)          // B format F16
-                               | ((256u >> 3) << 17)   // N
-                               | ((256u >> 4) << 24);  // M
+// Instruction descriptor, D = F32, A and B K-major, M = 256 (a CTA pair),
+// N = NT: kind::tf32 with A = B = TF32, kind::f16 with A = B = F16.
+template <int OP, int NT>
+constexpr uint32_t idesc() {
+    return (1u << 4)                                  // D format F32
+           | ((OP == kOpF16 ? 0u : 2u) << 7)          // A format F16 / TF32
+           | ((OP == kOpF16 ? 0u : 2u) << 10)         // B format F16 / TF32
+           | ((static_cast<uint32_t>(NT) >> 3) << 17)  // N
+           | ((256u >> 4) << 24);                     // M
+}
 
 // ------------------------------------------------------------- tcgen05 ops --
 
@@ -161,18 +166,19 @@ __device__ __forceinline__ void tc_fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// One M=256 x N=256 MMA over the CTA pair (K = 8 TF32 or 16 FP16 reals),
+// One M=256 x N=NT MMA over the CTA pair (K = 8 TF32 or 16 FP16 reals),
 // issued by the leader.
-template <int OP>
+template <int OP, int NT>
 __device__ __forceinline__ void mma_pair(uint32_t d_tmem, uint64_t a_desc,
                                          uint64_t b_desc, uint32_t accumulate) {
+    constexpr uint32_t kIdesc = idesc<OP, NT>();
     if constexpr (OP == kOpF16) {
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
             "setp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
                 d_tmem),
-            "l"(a_desc), "l"(b_desc), "r"(kIdescF16), "r"(accumulate)
+            "l"(a_desc), "l"(b_desc), "r"(kIdesc), "r"(accumulate)
             : "memory");
     } else {
         asm volatile(
@@ -180,7 +186,7 @@ __device__ __forceinline__ void mma_pair(uint32_t d_tmem, uint64_t a_desc,
             "setp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
                 d_tmem),
-            "l"(a_desc), "l"(b_desc), "r"(kIdescTf32), "r"(accumulate)
+            "l"(a_desc), "l"(b_desc), "r"(kIdesc), "r"(accumulate)
             : "memory");
     }
 }
@@ -283,8 +289,8 @@ struct GridGeom {
     int64_t n[3];        // x, y, z lengths (2-D: y is a dummy axis of length 1)
     int64_t off[3];      // offsets of the axes in the concatenated array
     int src[3];          // caller axis feeding x, y, z (-1: dummy)
-    int64_t blocks[3];   // table blocks along x (TX, even count), y (TY), z (256)
-    int tile[3];         // TX, TY, 256 with TX * TY = 128
+    int64_t blocks[3];   // table blocks along x (TX, even count), y (TY), z (NT)
+    int tile[3];         // TX, TY, NT with TX * TY = 128
     int64_t n_stages;    // padded modes / modes per stage
     int64_t n_modes;
     int ksteps;          // MMA K-steps per pipeline stage
@@ -383,8 +389,8 @@ __device__ __forceinline__ int amp_exponent(const unsigned int *amp_max) {
 // One thread per (axis point, mode), points fastest, FP32 only.  Axis x
 // writes w*Ex * 2^-e (amplitudes normalised below 1), axis y writes Ey
 // (complex FP32, blocked [block][stage][mode][tile]); axis z writes the
-// pre-split image of [Re Ez, Im Ez] in the operand format: per 256-point
-// block and stage, the half of each CTA of a pair (128 points) is one
+// pre-split image of [Re Ez, Im Ez] in the operand format: per NT-point
+// block and stage, the half of each CTA of a pair (NT / 2 points) is one
 // contiguous run of [K-step][hi, lo] blocks in the UMMA canonical K-major
 // layout.  The phase is reduced to turns exactly (gst_mixed.cuh) before the
 // FP32 sincospi.
@@ -454,14 +460,16 @@ __global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ mod
     } else if (axis == 1) {
         ey[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(c, s);
     } else {
-        const int rank = t / kCtaCols;
-        const uint32_t row = static_cast<uint32_t>(t % kCtaCols);
+        const int cta_cols = tile / 2;
+        const int bblk = b_block_bytes(tile);
+        const int rank = t / cta_cols;
+        const uint32_t row = static_cast<uint32_t>(t % cta_cols);
         const int kstep = mm / kMpk;
         const uint32_t k0 = 2u * (mm % kMpk);
-        const int64_t half_bytes = static_cast<int64_t>(g.ksteps) * 2 * kBlockBytes;
+        const int64_t half_bytes = static_cast<int64_t>(g.ksteps) * 2 * bblk;
         unsigned char *half = ez_image + ((blk * g.n_stages + st) * 2 + rank) * half_bytes;
-        unsigned char *bh = half + (kstep * 2 + 0) * kBlockBytes;
-        unsigned char *bl = half + (kstep * 2 + 1) * kBlockBytes;
+        unsigned char *bh = half + (kstep * 2 + 0) * bblk;
+        unsigned char *bl = half + (kstep * 2 + 1) * bblk;
         if constexpr (OP == kOpF16) {
             // (Re, Im) are adjacent in K: one 4-byte store per part
             const __half2 hi = __floats2half2_rn(c, s);
@@ -491,7 +499,7 @@ __device__ __forceinline__ int64_t ceil_div_dev(int64_t a, int64_t b) {
 
 struct GridArgs {
     GridGeom g;
-    int64_t pair_blocks[3];   // pair tiles along x (2 TX), y (TY), z (256)
+    int64_t pair_blocks[3];   // pair tiles along x (2 TX), y (TY), z (NT)
     // Work items: the first n_full pair tiles run whole; every later tile is
     // split into `split` (1 or 2) parts over its stages, and the parts add
     // their scaled sums into the (pre-zeroed) output, so the last partial
@@ -512,14 +520,14 @@ struct GridArgs {
 
 // One ring of pipeline slots per CTA: its half of B (bulk copy), its w*Ex
 // and Ey table slices (bulk copies) and its 128 rows of A (generated).
-template <int TY, int OP>
+template <int TY, int OP, int NT>
 struct StageLayout {
     static constexpr int TX = kCtaRows / TY;
     static constexpr int KS = ksteps_for(TY, OP);
     static constexpr int kModesPerStage = modes_per_stage(TY, OP);
     static constexpr int kChunkStages = chunk_modes(OP) / kModesPerStage;
     static constexpr int kAStageBytes = KS * 2 * kBlockBytes;
-    static constexpr int kBStageBytes = KS * 2 * kBlockBytes;   // per CTA
+    static constexpr int kBStageBytes = KS * 2 * b_block_bytes(NT);   // per CTA
     static constexpr int kWxBytes = kModesPerStage * TX * 8;
     static constexpr int kEyBytes = kModesPerStage * TY * 8;
     static constexpr int kB = 0;
@@ -534,15 +542,18 @@ struct StageLayout {
     static constexpr int kBars = kPipe * kSlot;
     static constexpr int kSmem = kBars + 1024 /*align*/ + 512 /*bars*/;
     static_assert(kPipe >= 3, "ring too shallow");
-    static_assert(kPipe * kSlot >= kCtaRows * (kTileCols + 4) * 4,
+    static_assert(kPipe * kSlot >= kCtaRows * (NT + 4) * 4,
                   "ring too small to stage a float32 tile");
     static_assert(kChunkStages >= 1, "chunk shorter than a stage");
 };
 
-template <int TY, int OP>
+template <int TY, int OP, int NT>
 __global__ void __launch_bounds__(kThreads, 1)
     grid_tc_kernel(const GridArgs a) {
-    using L = StageLayout<TY, OP>;
+    using L = StageLayout<TY, OP, NT>;
+    constexpr int kTileCols = NT;
+    constexpr int kColsPerThread = NT / 4;   // a quarter of an accumulator row
+    constexpr int kBBlock = b_block_bytes(NT);
     constexpr int TX = L::TX;
     constexpr int P = L::kPipe;
     constexpr int KS = L::KS;
@@ -728,14 +739,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const uint32_t d = tmem + buf * 256;
 #pragma unroll
                     for (int ks = 0; ks < KS; ++ks) {
-                        const uint64_t bh = slot_desc + ((L::kB + (ks * 2 + 0) * kBlockBytes) >> 4);
-                        const uint64_t bl = slot_desc + ((L::kB + (ks * 2 + 1) * kBlockBytes) >> 4);
+                        const uint64_t bh = slot_desc + ((L::kB + (ks * 2 + 0) * kBBlock) >> 4);
+                        const uint64_t bl = slot_desc + ((L::kB + (ks * 2 + 1) * kBBlock) >> 4);
                         const uint64_t ah = slot_desc + ((L::kA + (ks * 2 + 0) * kBlockBytes) >> 4);
                         const uint64_t al = slot_desc + ((L::kA + (ks * 2 + 1) * kBlockBytes) >> 4);
                         const uint32_t acc = (first && ks == 0) ? 0u : 1u;
-                        mma_pair<OP>(d, ah, bh, acc);
-                        mma_pair<OP>(d, ah, bl, 1u);
-                        mma_pair<OP>(d, al, bh, 1u);
+                        mma_pair<OP, NT>(d, ah, bh, acc);
+                        mma_pair<OP, NT>(d, ah, bl, 1u);
+                        mma_pair<OP, NT>(d, al, bh, 1u);
                     }
                     mma_commit_pair(&empty[s]);
                     if ((st % kChunkStages) == kChunkStages - 1 || st == n_st - 1)
@@ -901,18 +912,20 @@ __global__ void __launch_bounds__(kThreads, 1)
                                     sc * acc[i + 3]);
             }
             asm volatile("bar.sync 1, %0;" ::"n"(kGenThreads) : "memory");
-            constexpr int kF4PerRow = kTileCols / 4;            // 64
-            constexpr int kRowsPerPass = kGenThreads / kF4PerRow; // 8
+            constexpr int kF4PerRow = kTileCols / 4;              // 64 / 48 / 32
+            constexpr int kRowsPerPass = kGenThreads / kF4PerRow;  // 8 / 10 / 16
             const int c4 = gt % kF4PerRow;
+            if (gt < kRowsPerPass * kF4PerRow) {
 #pragma unroll 4
-            for (int r = gt / kF4PerRow; r < kCtaRows; r += kRowsPerPass) {
-                const int64_t x = xblk * TX + r / TY;
-                const int64_t y = yb * TY + r % TY;
-                if (x < g.n[0] && y < g.n[1]) {
-                    float *o = static_cast<float *>(a.out) + (x * g.n[1] + y) * nz_all +
-                               zb * kTileCols;
-                    reinterpret_cast<float4 *>(o)[c4] =
-                        *reinterpret_cast<const float4 *>(stage + r * kStride + 4 * c4);
+                for (int r = gt / kF4PerRow; r < kCtaRows; r += kRowsPerPass) {
+                    const int64_t x = xblk * TX + r / TY;
+                    const int64_t y = yb * TY + r % TY;
+                    if (x < g.n[0] && y < g.n[1]) {
+                        float *o = static_cast<float *>(a.out) +
+                                   (x * g.n[1] + y) * nz_all + zb * kTileCols;
+                        reinterpret_cast<float4 *>(o)[c4] = *reinterpret_cast<const float4 *>(
+                            stage + r * kStride + 4 * c4);
+                    }
                 }
             }
         } else if (ok) {
@@ -1001,8 +1014,8 @@ __global__ void zero_split_tiles_kernel(GridGeom g, GridArgs a, int64_t first_ti
     const int64_t x = xb * 2 * tx + r / ty;
     const int64_t y = yb * ty + r % ty;
     if (x >= g.n[0] || y >= g.n[1]) return;
-    const int64_t z0 = zb * kTileCols;
-    const int64_t nz = min(static_cast<int64_t>(kTileCols), g.n[2] - z0);
+    const int64_t z0 = zb * g.tile[2];
+    const int64_t nz = min(static_cast<int64_t>(g.tile[2]), g.n[2] - z0);
     const int64_t o = (x * g.n[1] + y) * g.n[2] + z0;
     for (int64_t z = lane; z < nz; z += 32) {
         if (a.out_f32)
@@ -1012,10 +1025,10 @@ __global__ void zero_split_tiles_kernel(GridGeom g, GridArgs a, int64_t first_ti
     }
 }
 
-template <int TY, int OP>
+template <int TY, int OP, int NT>
 cudaError_t launch_grid(const GridArgs &args, int64_t n_pairs, cudaStream_t s) {
-    using L = StageLayout<TY, OP>;
-    cudaError_t e = cudaFuncSetAttribute(grid_tc_kernel<TY, OP>,
+    using L = StageLayout<TY, OP, NT>;
+    cudaError_t e = cudaFuncSetAttribute(grid_tc_kernel<TY, OP, NT>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          L::kSmem);
     if (e != cudaSuccess) return e;
@@ -1031,9 +1044,37 @@ cudaError_t launch_grid(const GridArgs &args, int64_t n_pairs, cudaStream_t s) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, grid_tc_kernel<TY, OP>, args);
+    e = cudaLaunchKernelEx(&cfg, grid_tc_kernel<TY, OP, NT>, args);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
+}
+
+template <int TY, int OP>
+cudaError_t launch_grid_nt(const GridArgs &args, int64_t n_pairs, cudaStream_t s) {
+    switch (args.g.tile[2]) {
+        case 128: return launch_grid<TY, OP, 128>(args, n_pairs, s);
+        case 192: return launch_grid<TY, OP, 192>(args, n_pairs, s);
+        default: return launch_grid<TY, OP, 256>(args, n_pairs, s);
+    }
+}
+
+// z tile (MMA N) for an axis of nz points: the fewest tile-times, a tile
+// costing max(0.8, NT / 256) of a 256-wide one (below 0.8 the A generation,
+// which does not shrink with NT, sets the pace); then the fewest padded
+// columns (MMA work); then the wider tile.
+int pick_tile_cols(int64_t nz) {
+    int best = 256;
+    int64_t best_time = ceil_div(nz, 256) * 256, best_pad = ceil_div(nz, 256) * 256;
+    for (int nt : {192, 128}) {
+        const int64_t time = ceil_div(nz, nt) * std::max(205, nt);
+        const int64_t pad = ceil_div(nz, nt) * nt;
+        if (time < best_time || (time == best_time && pad < best_pad)) {
+            best = nt;
+            best_time = time;
+            best_pad = pad;
+        }
+    }
+    return best;
 }
 
 struct GridPlan {
@@ -1070,7 +1111,7 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
     }
     g.tile[0] = kCtaRows / p.ty;
     g.tile[1] = p.ty;
-    g.tile[2] = kTileCols;
+    g.tile[2] = pick_tile_cols(g.n[2]);
     p.pair_blocks[0] = ceil_div(g.n[0], 2 * g.tile[0]);
     p.pair_blocks[1] = ceil_div(g.n[1], g.tile[1]);
     p.pair_blocks[2] = ceil_div(g.n[2], g.tile[2]);
@@ -1090,7 +1131,7 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
     const size_t ey_bytes = static_cast<size_t>(g.blocks[1]) * g.n_stages *
                             per_stage * g.tile[1];
     const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages * 2 *
-                            g.ksteps * 2 * kBlockBytes;
+                            g.ksteps * 2 * b_block_bytes(g.tile[2]);
     p.pt_base1 = g.blocks[0] * g.tile[0];
     p.pt_base2 = p.pt_base1 + g.blocks[1] * g.tile[1];
     p.n_pt_total = p.pt_base2 + g.blocks[2] * g.tile[2];
@@ -1183,11 +1224,11 @@ int run_contract(const GridPlan &p, const unsigned char *ws, void *out,
     const int64_t n_items = args.n_full + (n_tiles - args.n_full) * split;
     cudaError_t e;
     if (p.g.op == kOpF16)
-        e = (p.ty == 16) ? launch_grid<16, kOpF16>(args, n_items, s)
-                         : launch_grid<1, kOpF16>(args, n_items, s);
+        e = (p.ty == 16) ? launch_grid_nt<16, kOpF16>(args, n_items, s)
+                         : launch_grid_nt<1, kOpF16>(args, n_items, s);
     else
-        e = (p.ty == 16) ? launch_grid<16, kOpTf32>(args, n_items, s)
-                         : launch_grid<1, kOpTf32>(args, n_items, s);
+        e = (p.ty == 16) ? launch_grid_nt<16, kOpTf32>(args, n_items, s)
+                         : launch_grid_nt<1, kOpTf32>(args, n_items, s);
     GST_TRY_CUDA(e);
     return GST_OK;
 }
@@ -1202,6 +1243,10 @@ extern "C" {
 int gst_grid_tc_set_operands(int kind) {
     if (kind != GST_TC_TF32 && kind != GST_TC_F16) return -1;
     return gst::g_operand_kind.exchange(kind);
+}
+
+int gst_grid_tc_tile_cols(int64_t nz) {
+    return nz < 0 ? -1 : gst::pick_tile_cols(nz);
 }
 
 int gst_grid_tc_workspace_size(int dim, int64_t n_modes,

@@ -227,6 +227,9 @@ int gst_summate_fourier_grid_tc(int dim, int64_t n_modes, const int64_t *axis_le
  * precomputation step). */
 int gst_grid_tc_workspace_size(int dim, int64_t n_modes,
                                const int64_t *axis_len, size_t *bytes);
+/* Width of the z tile (the MMA's N: 128, 192 or 256 points) the grid path
+ * uses for a last axis of nz points; -1 for nz < 0.  Informational. */
+int gst_grid_tc_tile_cols(int64_t nz);
 int gst_grid_tc_tables(int dim, int64_t n_modes, const int64_t *axis_len,
                        const double *axes, const double *cov_samples,
                        const double *z_1, const double *z_2, void *workspace,

@@ -62,6 +62,31 @@ def test_tc_3d(cuda_lib, shape, n_modes):
     assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (rms, mx)
 
 
+@pytest.mark.parametrize("nz,nt", [
+    (128, 128), (129, 192), (150, 192), (192, 192), (193, 256), (256, 256),
+    (320, 192), (384, 192), (640, 256), (40, 128)])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_tc_tile_widths(cuda_lib, nz, nt, dim):
+    """The z tile (MMA N = 128, 192 or 256) picked from the last axis: every
+    width against the oracle, on 2-D and 3-D grids, with partial last tiles
+    and both the staged (float32, whole tile) and the direct epilogue."""
+    n_modes = 150
+    cov, z1, z2 = case(nz + dim, dim, n_modes, k_scale=0.05)
+    lead = [np.arange(34.0) * 0.9] + ([np.arange(17.0) - 3.0] if dim == 3 else [])
+    axes = lead + [np.linspace(-10.0, 40.0, nz)]
+    from gstools_gb300 import _native
+
+    assert _native.grid_tile_cols(nz) == nt
+    for out_dtype in ("float32", "float64"):
+        got = gg.summate_grid(cov, z1, z2, axes, precision="mixed",
+                              method="tensor", out_dtype=out_dtype)
+        sub = [a[::3] for a in axes[:-1]] + [axes[-1]]
+        ref = grid_ref(cov, z1, z2, sub)
+        idx = tuple(slice(None, None, 3) for _ in axes[:-1]) + (slice(None),)
+        rms, mx = errors(got[idx], ref, n_modes)
+        assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (out_dtype, rms, mx)
+
+
 def test_tc_exp3d_workload_slab(cuda_lib, workloads):
     """The benchmark's modes (3-D anisotropic Exponential, 2000 modes) on a
     full 256^3 grid, checked against the oracle on scattered slabs."""
