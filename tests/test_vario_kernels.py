@@ -193,13 +193,13 @@ def test_gpu_unstructured_random(cuda_lib, dim, n, f_max, est):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["offset", "close_far_out", "bins64", "bins65"])
+@pytest.mark.parametrize("case", ["offset", "close_far_out", "bins1024", "bins1025"])
 def test_gpu_unstructured_fp32_distance_guard(cuda_lib, case):
     """The FP32 squared distance and its guard: integer coordinates far from
     the origin (every pair distance that is an integer hits an integer edge
     exactly), tiny distances between points at 3e8 (the quadratic guard
-    term), and the 64-bin limit of the private-histogram kernel and one bin
-    past it (shared-atomic kernel).  Counts exact, sums within 1e-12."""
+    term), and the 1024-bin limit of the fast kernel and one bin past it
+    (the general kernel).  Counts exact, sums within 1e-12."""
     import gstools_gb300.variogram as gv
 
     rng = np.random.RandomState(77)
@@ -212,7 +212,7 @@ def test_gpu_unstructured_fp32_distance_guard(cuda_lib, case):
         pos = base + np.round(rng.uniform(-5, 5, size=(3, n))) * 2.0 ** -22
         edges = np.arange(0.0, 12.0) * 2.0 ** -22
     else:
-        nb = 64 if case == "bins64" else 65
+        nb = 1024 if case == "bins1024" else 1025
         pos = rng.uniform(0, 100, size=(3, n))
         pos[:, : n // 2] = np.round(pos[:, : n // 2])
         edges = np.linspace(0.0, 100.0, nb + 1)
