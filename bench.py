@@ -749,6 +749,17 @@ def wl_vario(args, torch, gg, flush):
 
     t = _timed_events(torch, step, args.steps, args.warmup, flush)
     pairs = n * (n - 1) / 2
+    # directional: the two axes, tolerance pi/8, bandwidth 20
+    dirs = torch.tensor([[1.0, 0.0], [0.0, 1.0]], dtype=torch.float64, device=dev)
+    vario_d = torch.zeros(2 * nb, dtype=torch.float64, device=dev)
+    counts_d = torch.zeros(2 * nb, dtype=torch.int64, device=dev)
+
+    def step_dir():
+        _native.call("gst_vario_directional", 2, n, 1, p(dfd), nb, p(de), p(dp), 2,
+                     p(dirs), float(np.pi / 8), 20.0, 0, ord("m"), p(vario_d),
+                     p(counts_d), stream)
+
+    t_dir = _timed_events(torch, step_dir, args.steps, args.warmup, flush)
     sample = 3000
     t0 = time.perf_counter()
     go, co = oracle.c_vario_unstructured(f[:, :sample], edges, pos[:, :sample])
@@ -778,6 +789,9 @@ def wl_vario(args, torch, gg, flush):
                 "pairs_per_step": pairs, "bins": nb},
         error_vs_oracle={"max_rel": err, "counts_exact": exact_counts,
                          "points": sample},
+        directional={"value": pairs / t_dir / 1e9, "unit": "G pairs/s",
+                     "ms": t_dir * 1e3, "directions": 2, "angles_tol": "pi/8",
+                     "bandwidth": 20.0},
         axis_variogram={"value": axis_pairs / t_axis / 1e9, "unit": "G pairs/s",
                         "ms": t_axis * 1e3, "field": [na, na, na],
                         "kernel": "vario_structured_tiled_kernel",

@@ -106,6 +106,8 @@ SIGNATURES = {
                                       _ptr]),
     "gst_vario_unstructured": (_c_int, [_c_int, _i64, _i64, _ptr, _i64, _ptr, _ptr,
                                         _c_int, _c_int, _ptr, _ptr, _ptr]),
+    "gst_vario_angle_boundary": (_c_int, [_dbl, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double)]),
     "gst_vario_directional": (_c_int, [_c_int, _i64, _i64, _ptr, _i64, _ptr, _ptr,
                                        _i64, _ptr, _dbl, _dbl, _c_int, _c_int,
                                        _ptr, _ptr, _ptr]),

@@ -28,6 +28,7 @@
 // The structured estimator runs one CTA per (lag, column chunk), partial
 // sums reduced in a fixed order (deterministic).
 #include <algorithm>
+#include <cmath>
 
 #include "gst_common.cuh"
 
@@ -40,6 +41,17 @@ constexpr int kMaxDims = 3;
 
 __device__ __forceinline__ double estimate(int est, double d) {
     return est == 'c' ? sqrt(fabs(d)) : d * d;
+}
+
+// The reference's angle test, "if tt < 1: ok = acos(tt) < tol" with
+// tt = |s| / dist, decided exactly: with a correctly rounded acos,
+// RN(acos(tt)) < tol holds iff acos(tt) lies below the midpoint b of tol and
+// its predecessor, i.e. iff tt > cos(b) (acos decreases).  cos(b) is formed
+// once per call in double-double (angle_boundary) and compared here exactly,
+// so no device acos (whose last bit may differ from the host's) decides a
+// pair on the tolerance cone.  tt >= 1 always passes, as in the reference.
+__device__ __forceinline__ bool angle_ok(double tt, double c_hi, double c_lo) {
+    return tt > c_hi || (tt == c_hi && c_lo < 0.0);
 }
 
 __device__ __forceinline__ double haversine(double lat_j, double lon_j, double lat_k,
@@ -102,6 +114,7 @@ struct VarioArgs {
     int d_max;            // 0: omnidirectional
     const double *dirs;   // d_max x dim (unit vectors)
     double angles_tol;
+    double cos_hi, cos_lo;   // angle test boundary, see angle_boundary()
     double bandwidth;
     int separate_dirs;
     double *sums;         // max(d_max, 1) x n_bins, raw sums
@@ -201,10 +214,7 @@ __global__ void __launch_bounds__(kVarioThreads)
                     }
                     ok = b_dist < __dmul_rn(a.bandwidth, a.bandwidth);
                 }
-                if (ok && dist > 0.0) {
-                    const double tt = fabs(s_prod) / dist;
-                    if (tt < 1.0) ok = acos(tt) < a.angles_tol;
-                }
+                if (ok && dist > 0.0) ok = angle_ok(fabs(s_prod) / dist, a.cos_hi, a.cos_lo);
                 if (!ok) continue;
                 for (int64_t m = 0; m < a.f_max; ++m) {
                     const double fa = a.f[m * a.n + k], fb = a.f[m * a.n + j];
@@ -253,6 +263,9 @@ constexpr float kGuardRel = 1.9073486328125e-06f;     // 2^-19
 constexpr float kGuardAbs = 4.547473508864641e-13f;   // 2^-41
 constexpr float kGuardSq = 3.2311742677852644e-27f;   // 2^-88
 
+constexpr int kOmniMaxDirs = 32;
+constexpr float kDirGuardAbs = 2.2737367544323206e-13f;   // 2^-42
+
 struct OmniArgs {
     int64_t n;
     int64_t f_max;
@@ -263,11 +276,19 @@ struct OmniArgs {
     int est;
     int64_t n_tiles;      // 128-point tiles per axis
     int64_t n_tri;        // upper-triangle tiles
-    double *sums;
+    double *sums;         // max(d_max, 1) x n_bins
     unsigned long long *counts;
+    // directional estimator (d_max > 0): unit directions, angle tolerance
+    // in (0, pi], bandwidth (<= 0: none), first matching direction only
+    int d_max;
+    const double *dirs;   // d_max x dim
+    double angles_tol;
+    double cos_hi, cos_lo;   // angle test boundary, see angle_boundary()
+    double bandwidth;
+    int separate_dirs;
 };
 
-__host__ __device__ constexpr size_t omni_smem_bytes(int nb) {
+__host__ __device__ constexpr size_t omni_smem_bytes(int nb, int nh) {
     return sizeof(double) * (nb + 1)                        // edges
            + sizeof(float) * 2 * (nb + 1)                   // squared edges, guards
            + sizeof(float4) * kOmniThreads * 2              // k-tile hi/lo, |x| max
@@ -276,7 +297,8 @@ __host__ __device__ constexpr size_t omni_smem_bytes(int nb) {
            + sizeof(double) * kOmniThreads                  // field 0 at j, per lane
            + sizeof(unsigned int) * 2 * kOmniThreads        // per-warp queues (64)
            + sizeof(short) * kOmniTab                       // bin table
-           + (sizeof(double) + sizeof(unsigned int)) * nb * kOmniWarps;
+           + sizeof(float) * 3 * kOmniMaxDirs               // FP32 directions
+           + (sizeof(double) + sizeof(unsigned int)) * nh * kOmniWarps;
 }
 
 __device__ __forceinline__ void tile_of(int64_t t, int64_t &jt, int64_t &kt) {
@@ -351,16 +373,141 @@ __device__ __forceinline__ int pair_bin(int kl, const float *jh, const float *jl
     return bin;
 }
 
+// Directional form of pair_bin: the bin (or -1) and, in `mask`, the
+// directions that accept the pair (bit dd; only the first with
+// separate_dirs).  The FP32 projections decide unless a quantity lies within
+// its guard of a threshold: the angle test |s| / dist > cos(tol) within
+// 2^-19 + 2^-42 X / dist, the bandwidth test within the distance guard at
+// d2; then the whole pair is evaluated in FP64 the reference's way
+// (unfused sums, acos of |s| / dist against the tolerance).
+template <int DIM>
+__device__ __forceinline__ int pair_bin_dirs(int kl, const float *jh, const float *jl,
+                                             const double *pj, const float4 *k_hi,
+                                             const float4 *k_lo, const float *e2f,
+                                             const float *guard, const double *edges,
+                                             int nb, float lim, const short *tab,
+                                             float tscale, bool exact_only, float X,
+                                             const float *dirf, const OmniArgs &a,
+                                             float ctol, float bw2f, int64_t k,
+                                             unsigned int &mask) {
+    mask = 0u;
+    bool exact = exact_only;
+    int bin = -1;
+    if (!exact) {
+        const float4 kh = k_hi[kl], klo = k_lo[kl];
+        float dx[3] = {0.f, 0.f, 0.f};
+        dx[0] = (jh[0] - kh.x) + (jl[0] - klo.x);
+        float f2 = dx[0] * dx[0];
+        if (DIM > 1) {
+            dx[1] = (jh[1] - kh.y) + (jl[1] - klo.y);
+            f2 = fmaf(dx[1], dx[1], f2);
+        }
+        if (DIM > 2) {
+            dx[2] = (jh[2] - kh.z) + (jl[2] - klo.z);
+            f2 = fmaf(dx[2], dx[2], f2);
+        }
+        if (!(f2 <= lim)) return -1;
+        int lo = tab[min(__float2int_rz(f2 * tscale), kOmniTab - 1)];
+        while (lo >= 0 && e2f[lo] > f2) --lo;
+        while (lo < nb && e2f[lo + 1] <= f2) ++lo;
+        exact = (lo >= 0 && fabsf(f2 - e2f[lo]) <= guard[lo]) ||
+                (lo + 1 <= nb && fabsf(f2 - e2f[lo + 1]) <= guard[lo + 1]);
+        bin = (lo >= 0 && lo < nb) ? lo : -1;
+        if (!exact && bin < 0) return -1;
+        if (!exact && !(f2 >= 1e-30f)) exact = true;   // (near) zero distance
+        if (!exact) {
+            const float dist = sqrtf(f2);
+            const float gx = kGuardRel + kDirGuardAbs * X / dist;
+            const float gb = kGuardRel * f2 + kGuardAbs * X * dist + kGuardSq * X * X;
+            for (int dd = 0; dd < a.d_max; ++dd) {
+                const float *dv = dirf + 3 * dd;
+                float sp = dx[0] * dv[0];
+                if (DIM > 1) sp = fmaf(dx[1], dv[1], sp);
+                if (DIM > 2) sp = fmaf(dx[2], dv[2], sp);
+                bool ok = true;
+                if (bw2f > 0.0f) {
+                    float b = 0.0f;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) {
+                        const float t = dx[d] - sp * dv[d];
+                        b = fmaf(t, t, b);
+                    }
+                    if (fabsf(b - bw2f) <= gb) {
+                        exact = true;
+                        break;
+                    }
+                    ok = b < bw2f;
+                }
+                if (ok) {
+                    const float x = fabsf(sp) / dist;
+                    if (fabsf(x - ctol) <= gx) {
+                        exact = true;
+                        break;
+                    }
+                    ok = x > ctol;
+                }
+                if (ok) {
+                    mask |= 1u << dd;
+                    if (a.separate_dirs) break;
+                }
+            }
+        }
+    }
+    if (exact) {
+        mask = 0u;
+        double diffv[3] = {0.0, 0.0, 0.0};
+        double d2 = 0.0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            diffv[d] = pj[d] - a.pos[d * a.n + k];
+            d2 = __dadd_rn(d2, __dmul_rn(diffv[d], diffv[d]));
+        }
+        if (!(d2 >= 0.0)) return -1;
+        const double dist = sqrt(d2);
+        int lo = -1, hi = nb + 1;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (edges[mid] <= dist) lo = mid; else hi = mid;
+        }
+        if (lo < 0 || lo >= nb) return -1;
+        bin = lo;
+        for (int dd = 0; dd < a.d_max; ++dd) {
+            const double *dir = a.dirs + dd * DIM;
+            double s_prod = 0.0;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                s_prod = __dadd_rn(s_prod, __dmul_rn(diffv[d], dir[d]));
+            bool ok = true;
+            if (a.bandwidth > 0.0) {
+                double b_dist = 0.0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const double tt = __dsub_rn(diffv[d], __dmul_rn(s_prod, dir[d]));
+                    b_dist = __dadd_rn(b_dist, __dmul_rn(tt, tt));
+                }
+                ok = b_dist < __dmul_rn(a.bandwidth, a.bandwidth);
+            }
+            if (ok && dist > 0.0) ok = angle_ok(fabs(s_prod) / dist, a.cos_hi, a.cos_lo);
+            if (ok) {
+                mask |= 1u << dd;
+                if (a.separate_dirs) break;
+            }
+        }
+    }
+    return mask != 0u ? bin : -1;
+}
+
 template <bool CRESSIE>
 __device__ __forceinline__ double estimate_t(double d) {
     return CRESSIE ? sqrt(fabs(d)) : d * d;
 }
 
-template <int DIM, bool CRESSIE>
+template <int DIM, bool CRESSIE, bool DIRS>
 __global__ void __launch_bounds__(kOmniThreads, 8)
     vario_omni_kernel(const OmniArgs a) {
     extern __shared__ __align__(16) double sh[];
     const int nb = a.n_bins;
+    const int nh = DIRS ? a.d_max * nb : nb;   // histogram cells: direction x bin
     const int tid = threadIdx.x;
     double *edges = sh;
     float *e2f = reinterpret_cast<float *>(edges + (nb + 1));
@@ -374,15 +521,22 @@ __global__ void __launch_bounds__(kOmniThreads, 8)
     double *w_fj = reinterpret_cast<double *>(w_max + 4);
     unsigned int *w_queue = reinterpret_cast<unsigned int *>(w_fj + kOmniThreads);
     double *h_sum = reinterpret_cast<double *>(w_queue + 2 * kOmniThreads);
-    unsigned int *h_cnt = reinterpret_cast<unsigned int *>(h_sum + nb * kOmniWarps);
-    short *tab = reinterpret_cast<short *>(h_cnt + nb * kOmniWarps);
+    unsigned int *h_cnt = reinterpret_cast<unsigned int *>(h_sum + nh * kOmniWarps);
+    short *tab = reinterpret_cast<short *>(h_cnt + nh * kOmniWarps);
+    float *dirf = reinterpret_cast<float *>(tab + kOmniTab);   // [dir][3]
+    const float ctol = DIRS ? static_cast<float>(cos(a.angles_tol)) : 0.0f;
+    const float bw2f =
+        (DIRS && a.bandwidth > 0.0) ? static_cast<float>(a.bandwidth * a.bandwidth) : 0.0f;
+    if (DIRS)
+        for (int i = tid; i < 3 * a.d_max; i += kOmniThreads)
+            dirf[i] = (i % 3 < DIM) ? static_cast<float>(a.dirs[(i / 3) * DIM + i % 3]) : 0.0f;
 
     for (int i = tid; i <= nb; i += kOmniThreads) {
         const double e = a.edges[i];
         edges[i] = e;
         e2f[i] = e > 0.0 ? __double2float_rn(e * e) : -1.0f;
     }
-    for (int i = tid; i < nb * kOmniWarps; i += kOmniThreads) {
+    for (int i = tid; i < nh * kOmniWarps; i += kOmniThreads) {
         h_sum[i] = 0.0;
         h_cnt[i] = 0u;
     }
@@ -406,14 +560,14 @@ __global__ void __launch_bounds__(kOmniThreads, 8)
 
     auto flush = [&]() {
         __syncthreads();
-        for (int b = tid; b < nb; b += kOmniThreads) {
+        for (int b = tid; b < nh; b += kOmniThreads) {
             double g = 0.0;
             unsigned long long c = 0ull;
             for (int w = 0; w < kOmniWarps; ++w) {
-                g += h_sum[w * nb + b];
-                c += h_cnt[w * nb + b];
-                h_sum[w * nb + b] = 0.0;
-                h_cnt[w * nb + b] = 0u;
+                g += h_sum[w * nh + b];
+                c += h_cnt[w * nh + b];
+                h_sum[w * nh + b] = 0.0;
+                h_cnt[w * nh + b] = 0u;
             }
             if (c != 0ull) {
                 atomicAdd(&a.sums[b], g);
@@ -506,37 +660,55 @@ __global__ void __launch_bounds__(kOmniThreads, 8)
                     __syncwarp();
                     const unsigned int e = q[lane];
                     const double d = k_f[(e >> 5) & 127u] - w_fj[warp * 32 + (e & 31u)];
-                    atomicAdd(&h_sum[warp * nb + (e >> 16)], estimate_t<CRESSIE>(d));
-                    atomicAdd(&h_cnt[warp * nb + (e >> 16)], 1u);
+                    atomicAdd(&h_sum[warp * nh + (e >> 16)], estimate_t<CRESSIE>(d));
+                    atomicAdd(&h_cnt[warp * nh + (e >> 16)], 1u);
                     __syncwarp();
                     if (lane < qn - 32) q[lane] = q[32 + lane];
                     __syncwarp();
                     qn -= 32;
                 }
             };
-            auto bin_of = [&](int kl) {
-                if (kl < kl1 && row_ok && (jt != kt || kl > tid) && k_hi[kl].w != 0.f)
+            // bin of pair (j, k), and its accepted directions (DIRS)
+            auto bin_of = [&](int kl, unsigned int &mask) {
+                mask = 1u;
+                if (kl < kl1 && row_ok && (jt != kt || kl > tid) && k_hi[kl].w != 0.f) {
+                    if (DIRS)
+                        return pair_bin_dirs<DIM>(kl, jh, jl, pj, k_hi, k_lo, e2f, guard,
+                                                  edges, nb, lim, tab, tscale, exact_only,
+                                                  X, dirf, a, ctol, bw2f,
+                                                  kt * kOmniThreads + kl, mask);
                     return pair_bin<DIM>(kl, jh, jl, pj, k_hi, k_lo, e2f, guard, edges, nb,
                                          lim, tab, tscale, exact_only, a.pos, a.n,
                                          kt * kOmniThreads + kl);
+                }
                 return -1;
+            };
+            // one queue entry per accepted direction (cell dir * nb + bin)
+            auto enqueue_dirs = [&](int bin, unsigned int mask, int kl) {
+                if constexpr (DIRS) {
+                    for (int dd = 0; dd < a.d_max; ++dd)
+                        enqueue((bin >= 0 && ((mask >> dd) & 1u)) ? dd * nb + bin : -1, kl);
+                } else {
+                    enqueue(bin, kl);
+                }
             };
             if (__any_sync(0xffffffffu, row_ok)) {
                 // two independent pairs per step for latency hiding (four
                 // measured no faster)
                 for (int kl = kl_first; kl < kl1; kl += 2) {
-                    const int b0 = bin_of(kl);
-                    const int b1 = bin_of(kl + 1);
-                    enqueue(b0, kl);
-                    enqueue(b1, kl + 1);
+                    unsigned int m0, m1;
+                    const int b0 = bin_of(kl, m0);
+                    const int b1 = bin_of(kl + 1, m1);
+                    enqueue_dirs(b0, m0, kl);
+                    enqueue_dirs(b1, m1, kl + 1);
                 }
             }
             __syncwarp();
             if (lane < qn) {
                 const unsigned int e = q[lane];
                 const double d = k_f[(e >> 5) & 127u] - w_fj[warp * 32 + (e & 31u)];
-                atomicAdd(&h_sum[warp * nb + (e >> 16)], estimate_t<CRESSIE>(d));
-                atomicAdd(&h_cnt[warp * nb + (e >> 16)], 1u);
+                atomicAdd(&h_sum[warp * nh + (e >> 16)], estimate_t<CRESSIE>(d));
+                atomicAdd(&h_cnt[warp * nh + (e >> 16)], 1u);
             }
         } else if (j < a.n) {
             // no field or several fields: per-lane terms
@@ -544,9 +716,13 @@ __global__ void __launch_bounds__(kOmniThreads, 8)
             const int kl0 = (jt == kt) ? tid + 1 : 0;
             for (int kl = kl0; kl < kl1; ++kl) {
                 const int64_t k = kt * kOmniThreads + kl;
-                const int bin = pair_bin<DIM>(kl, jh, jl, pj, k_hi, k_lo, e2f, guard, edges,
-                                              nb, lim, tab, tscale, exact_only, a.pos,
-                                              a.n, k);
+                unsigned int mask = 1u;
+                const int bin =
+                    DIRS ? pair_bin_dirs<DIM>(kl, jh, jl, pj, k_hi, k_lo, e2f, guard, edges,
+                                              nb, lim, tab, tscale, exact_only, X, dirf, a,
+                                              ctol, bw2f, k, mask)
+                         : pair_bin<DIM>(kl, jh, jl, pj, k_hi, k_lo, e2f, guard, edges, nb,
+                                         lim, tab, tscale, exact_only, a.pos, a.n, k);
                 if (bin < 0) continue;
                 double g = 0.0;
                 unsigned int c = 0u;
@@ -561,8 +737,11 @@ __global__ void __launch_bounds__(kOmniThreads, 8)
                     ++c;
                 }
                 if (c != 0u) {
-                    atomicAdd(&h_sum[(tid >> 5) * nb + bin], g);
-                    atomicAdd(&h_cnt[(tid >> 5) * nb + bin], c);
+                    for (int dd = 0; dd < (DIRS ? a.d_max : 1); ++dd) {
+                        if (!((mask >> dd) & 1u)) continue;
+                        atomicAdd(&h_sum[(tid >> 5) * nh + dd * nb + bin], g);
+                        atomicAdd(&h_cnt[(tid >> 5) * nh + dd * nb + bin], c);
+                    }
                 }
             }
         }
@@ -699,37 +878,112 @@ __global__ void vario_structured_finish(int64_t n0, int64_t n_chunks, int est,
     vario[k] = normalise(est, g, c);
 }
 
-template <int DIM, bool CRESSIE>
+// ---------------------------------------------- double-double angle bound --
+
+struct DD {
+    double hi, lo;
+};
+
+DD dd_two_sum(double a, double b) {
+    const double s = a + b;
+    const double bb = s - a;
+    return DD{s, (a - (s - bb)) + (b - bb)};
+}
+
+DD dd_add(DD a, DD b) {
+    DD s = dd_two_sum(a.hi, b.hi);
+    s.lo += a.lo + b.lo;
+    return dd_two_sum(s.hi, s.lo);
+}
+
+DD dd_mul(DD a, DD b) {
+    const double p = a.hi * b.hi;
+    const double e = std::fma(a.hi, b.hi, -p) + (a.hi * b.lo + a.lo * b.hi);
+    return dd_two_sum(p, e);
+}
+
+DD dd_div_d(DD a, double d) {
+    const double q1 = a.hi / d;
+    // remainder a - q1 d, exact in double-double
+    const double p = q1 * d;
+    const double e = std::fma(q1, d, -p);
+    const double r = ((a.hi - p) - e) + a.lo;
+    const double q2 = r / d;
+    return dd_two_sum(q1, q2);
+}
+
+// cos(tol - delta) in double-double, delta half the gap from tol down to the
+// next double: the boundary of "RN(acos(tt)) < tol".  Taylor series in
+// double-double (|x| <= 2, terms below 1e-40 dropped).  tol <= 0 or NaN:
+// only tt >= 1 passes; tol > 2 (beyond pi / 2 + 0.4): every tt in [0, 1]
+// passes.
+void angle_boundary(double tol, double &c_hi, double &c_lo) {
+    if (!(tol > 0.0)) {
+        c_hi = 1.0;
+        c_lo = -1e-30;
+        return;
+    }
+    if (tol > 2.0) {
+        c_hi = -2.0;
+        c_lo = 0.0;
+        return;
+    }
+    const double below = std::nextafter(tol, 0.0);
+    const DD x = dd_two_sum(tol, -(tol - below) * 0.5);   // exact: tol - delta
+    const DD x2 = dd_mul(x, x);
+    DD sum{1.0, 0.0}, term{1.0, 0.0};
+    for (int n = 1; n < 40; ++n) {
+        term = dd_div_d(dd_mul(term, x2), static_cast<double>((2 * n - 1) * (2 * n)));
+        const DD signed_term = (n & 1) ? DD{-term.hi, -term.lo} : term;
+        sum = dd_add(sum, signed_term);
+        if (std::fabs(term.hi) < 1e-40) break;
+    }
+    c_hi = sum.hi;
+    c_lo = sum.lo;
+}
+
+template <int DIM, bool CRESSIE, bool DIRS>
 cudaError_t launch_omni_t(const OmniArgs &o, cudaStream_t s) {
-    const size_t smem = omni_smem_bytes(o.n_bins) + 16;
-    cudaError_t e = cudaFuncSetAttribute(vario_omni_kernel<DIM, CRESSIE>,
+    const int nh = DIRS ? o.d_max * o.n_bins : o.n_bins;
+    const size_t smem = omni_smem_bytes(o.n_bins, nh) + 16;
+    cudaError_t e = cudaFuncSetAttribute(vario_omni_kernel<DIM, CRESSIE, DIRS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, vario_omni_kernel<DIM, CRESSIE>, kOmniThreads, smem);
+        &per_sm, vario_omni_kernel<DIM, CRESSIE, DIRS>, kOmniThreads, smem);
     if (e != cudaSuccess) return e;
     const int64_t grid = std::min<int64_t>(
         o.n_tri, static_cast<int64_t>(std::max(per_sm, 1)) * sm_count());
-    vario_omni_kernel<DIM, CRESSIE>
+    vario_omni_kernel<DIM, CRESSIE, DIRS>
         <<<static_cast<unsigned>(grid), kOmniThreads, smem, s>>>(o);
     return cudaGetLastError();
 }
 
 template <int DIM>
 cudaError_t launch_omni(const OmniArgs &o, cudaStream_t s) {
-    return o.est == 'c' ? launch_omni_t<DIM, true>(o, s) : launch_omni_t<DIM, false>(o, s);
+    if (o.d_max > 0)
+        return o.est == 'c' ? launch_omni_t<DIM, true, true>(o, s)
+                            : launch_omni_t<DIM, false, true>(o, s);
+    return o.est == 'c' ? launch_omni_t<DIM, true, false>(o, s)
+                        : launch_omni_t<DIM, false, false>(o, s);
 }
 
 int pairs_impl(const VarioArgs &args, double *vario, int64_t *counts, cudaStream_t s) {
     const int nh = (args.d_max > 0 ? args.d_max : 1) * args.n_bins;
     VarioArgs a = args;
+    angle_boundary(a.angles_tol, a.cos_hi, a.cos_lo);
     a.sums = vario;   // raw sums, normalised in place at the end
     a.counts = reinterpret_cast<unsigned long long *>(counts);
     GST_TRY_CUDA(cudaMemsetAsync(a.sums, 0, sizeof(double) * nh, s));
     GST_TRY_CUDA(cudaMemsetAsync(a.counts, 0, sizeof(unsigned long long) * nh, s));
-    if (a.d_max == 0 && !a.haversine && a.n_bins <= kOmniMaxBins) {
+    // Fast path: Euclidean; omnidirectional, or up to 32 directions with an
+    // angle tolerance in (0, pi]; at most 1024 histogram cells.
+    const bool fast_dirs =
+        a.d_max == 0 || (a.d_max <= kOmniMaxDirs && a.angles_tol > 0.0 &&
+                         a.angles_tol <= 3.14159265358979323846);
+    if (!a.haversine && fast_dirs && nh <= kOmniMaxBins) {
         OmniArgs o{};
         o.n = a.n;
         o.f_max = a.f_max;
@@ -742,6 +996,13 @@ int pairs_impl(const VarioArgs &args, double *vario, int64_t *counts, cudaStream
         o.n_tri = o.n_tiles * (o.n_tiles + 1) / 2;
         o.sums = a.sums;
         o.counts = a.counts;
+        o.d_max = a.d_max;
+        o.dirs = a.dirs;
+        o.angles_tol = a.angles_tol;
+        o.cos_hi = a.cos_hi;
+        o.cos_lo = a.cos_lo;
+        o.bandwidth = a.bandwidth;
+        o.separate_dirs = a.separate_dirs;
         if (o.n_tri > 0) {
             cudaError_t e = a.dim == 1   ? launch_omni<1>(o, s)
                             : a.dim == 2 ? launch_omni<2>(o, s)
@@ -840,6 +1101,12 @@ int gst_vario_directional(int dim, int64_t n, int64_t f_max, const double *f,
     a.bandwidth = bandwidth;
     a.separate_dirs = separate_dirs ? 1 : 0;
     return gst::pairs_impl(a, vario, counts, static_cast<cudaStream_t>(stream));
+}
+
+int gst_vario_angle_boundary(double angles_tol, double *cos_hi, double *cos_lo) {
+    if (cos_hi == nullptr || cos_lo == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    gst::angle_boundary(angles_tol, *cos_hi, *cos_lo);
+    return GST_OK;
 }
 
 int gst_vario_structured(int64_t n0, int64_t rest, const double *f,

@@ -371,6 +371,13 @@ int gst_vario_directional(int dim, int64_t n, int64_t f_max, const double *f,
                           double bandwidth, int separate_dirs, int estimator,
                           double *vario, int64_t *counts, void *stream);
 /* Variogram along axis 0 of f (n0 x rest, row-major), lags 0 .. n0 - 1;   */
+/* The directional estimators' angle test, the reference's
+ * "acos(|s| / dist) < angles_tol", is decided exactly as
+ * "|s| / dist > cos(b)" with b the midpoint of angles_tol and the next double
+ * below it (the decision of a correctly rounded acos); this returns cos(b) as
+ * a double-double (hi + lo).  Host-only, informational (no device needed). */
+int gst_vario_angle_boundary(double angles_tol, double *cos_hi, double *cos_lo);
+
 /* mask (n0 x rest bytes, nonzero = masked) may be NULL.  Deterministic.    */
 int gst_vario_structured(int64_t n0, int64_t rest, const double *f,
                          const unsigned char *mask, int estimator, double *vario,

@@ -172,6 +172,36 @@ def test_gpu_matches_recorded_cases(cuda_lib, ref_goldens):
                                        err_msg=name)
 
 
+def test_angle_boundary_double_double():
+    """cos of the rounding boundary of the angle tolerance (host code of the
+    library, no device): against 200-bit arithmetic, and the decisions it
+    gives on the 45-degree lattice pairs equal the host libm's acos test."""
+    import ctypes
+    import math
+
+    mpmath = pytest.importorskip("mpmath")
+    from gstools_gb300 import _native
+
+    lib = _native.load()
+    mpmath.mp.prec = 200
+    hi, lo = ctypes.c_double(), ctypes.c_double()
+    for tol in (math.pi / 4, math.pi / 8, 0.3, math.pi / 2, 1e-5, 1.9, 0.05):
+        assert lib.gst_vario_angle_boundary(tol, ctypes.byref(hi), ctypes.byref(lo)) == 0
+        b = mpmath.mpf(tol) - (mpmath.mpf(tol) - mpmath.mpf(math.nextafter(tol, 0.0))) / 2
+        assert abs(mpmath.mpf(hi.value) + mpmath.mpf(lo.value) - mpmath.cos(b)) < 1e-31
+    lib.gst_vario_angle_boundary(math.pi / 4, ctypes.byref(hi), ctypes.byref(lo))
+    for k in range(1, 40):
+        tt = k / math.sqrt(2.0 * k * k)
+        gpu_rule = tt > hi.value or (tt == hi.value and lo.value < 0.0)
+        assert gpu_rule == (tt >= 1.0 or math.acos(tt) < math.pi / 4), k
+    # tol <= 0 or NaN: only tt >= 1 passes; tol > 2: everything passes
+    for tol in (0.0, -1.0, float("nan")):
+        lib.gst_vario_angle_boundary(tol, ctypes.byref(hi), ctypes.byref(lo))
+        assert not (1.0 - 2**-53 > hi.value) and (1.0 > hi.value or lo.value < 0.0)
+    lib.gst_vario_angle_boundary(2.5, ctypes.byref(hi), ctypes.byref(lo))
+    assert 0.0 > hi.value
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("dim,n,f_max,est", [
     (1, 1, 1, "m"), (1, 500, 1, "c"), (2, 3000, 2, "m"), (3, 2000, 3, "c"),
@@ -241,6 +271,54 @@ def test_gpu_structured_tiled_limits(cuda_lib, shape):
         np.testing.assert_allclose(gv.ma_structured(fld, mask, est),
                                    oracle.c_vario_structured(fld, est, mask=mask),
                                    rtol=REL)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["grid45", "random", "offset", "fallback_tol0",
+                                  "fallback_cells"])
+def test_gpu_directional_fast_path(cuda_lib, case):
+    """Directional estimator on the FP32 fast path: an integer grid with the
+    angle tolerance exactly pi/4 from the axis directions (pairs on the
+    tolerance cone are decided in FP64 the reference's way), random points
+    with several tolerances and bandwidths, points far from the origin; and
+    the general kernel for a zero tolerance and for more than 1024
+    histogram cells."""
+    import gstools_gb300.variogram as gv
+
+    rng = np.random.RandomState(len(case))
+    if case == "grid45":
+        g1 = np.arange(20.0)
+        pos = np.array(np.meshgrid(g1, g1, indexing="ij")).reshape(2, -1)
+        dirs = np.array([[1.0, 0.0], [0.0, 1.0]])
+        runs = [(np.pi / 4, -1.0), (np.pi / 4, 1.0), (np.pi / 8, 2.0)]
+        edges = np.arange(0.0, 15.0, 1.0)
+    elif case in ("random", "offset"):
+        pos = rng.uniform(0, 40, size=(3, 1200))
+        if case == "offset":
+            pos += 1e6
+        dirs = rng.normal(size=(4, 3))
+        dirs /= np.linalg.norm(dirs, axis=1)[:, None]
+        runs = [(0.3, -1.0), (0.7, 5.0), (np.pi, 3.0), (np.pi / 2, -1.0)]
+        edges = np.linspace(0.0, 30.0, 21)
+    elif case == "fallback_tol0":
+        pos = rng.uniform(0, 10, size=(2, 300))
+        dirs = np.array([[1.0, 0.0]])
+        runs = [(0.0, -1.0)]
+        edges = np.linspace(0.0, 10.0, 11)
+    else:
+        pos = rng.uniform(0, 10, size=(2, 300))
+        dirs = np.array([[1.0, 0.0], [0.0, 1.0]])
+        runs = [(0.4, -1.0)]
+        edges = np.linspace(0.0, 10.0, 514)   # 2 x 513 cells
+    f = rng.normal(size=(1, pos.shape[1]))
+    f[0, ::13] = np.nan
+    for tol, bw in runs:
+        for separate in (False, True):
+            g, c = gv.directional(f, edges, pos, dirs, tol, bw, separate, "m")
+            go, co = oracle.c_vario_directional(f, edges, pos, dirs, tol, bw,
+                                                separate, "m")
+            np.testing.assert_array_equal(c, co, err_msg=f"{tol} {bw} {separate}")
+            np.testing.assert_allclose(g, go, rtol=REL, atol=0)
 
 
 @pytest.mark.gpu
