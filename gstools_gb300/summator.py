@@ -313,8 +313,9 @@ def summate_grid(cov_samples, z_1, z_2, axes, *, precision=None,
     ``method`` picks the kernel:
 
     * ``"pointwise"`` -- per-point phases (FP64 or mixed, per ``precision``);
-    * ``"tensor"``    -- the separable 3xTF32 tensor-core contraction (2-D and
-      3-D grids, requires ``precision="mixed"``);
+    * ``"tensor"``    -- the separable tensor-core contraction (three-product
+      FP16 split by default, 3xTF32 selectable; 2-D and 3-D grids, requires
+      ``precision="mixed"``);
     * ``"auto"``      -- ``"tensor"`` for mixed precision on 2-D / 3-D grids,
       ``"pointwise"`` otherwise.
     """

@@ -1,4 +1,5 @@
-"""GPU parity of the separable tensor-core grid path (3xTF32, tcgen05).
+"""GPU parity of the separable tensor-core grid path (tcgen05; three-product
+FP16 split by default, 3xTF32 selectable).
 
 Bar: RMS(gpu - oracle) of the scaled field <= 1e-5 sigma (sigma = sqrt(var),
 field scaled by sqrt(var / N)), and max error <= 1e-4 sigma.
