@@ -644,6 +644,30 @@ def _line(args, workload, value, t_step, dtype, config, **extra):
     return line
 
 
+def _cpu_sample(fn, items, work_of, target_s=5.0, what="items"):
+    """Time the oracle (all host cores) on the first items of a workload,
+    growing the sample until it runs about target_s seconds or covers every
+    item; returns a cpu_baseline dict in G mode*point/s."""
+    import oracle
+
+    oracle.build()
+    done, t, n = 0, 0.0, 1
+    while True:
+        n = min(n, len(items))
+        t0 = time.perf_counter()
+        for it in items[:n]:
+            fn(it)
+        t = time.perf_counter() - t0
+        done = sum(work_of(it) for it in items[:n])
+        if t >= target_s * 0.3 or n == len(items):
+            break
+        n = max(n + 1, int(n * min(8.0, target_s / max(t, 1e-3))))
+    return {"value": done / t / 1e9, "unit": UNIT, "cores": oracle.num_threads(),
+            "kind": "port",
+            "sample": f"FP64 C/OpenMP oracle on the first {n} of {len(items)} {what} "
+                      f"({done:.3g} mode*point, {t:.2f} s)"}
+
+
 def wl_krige(args, torch, gg, flush):
     """Ordinary kriging with an exponential covariance (var 1, length scale
     50): 1000 conditioning points and 65 536 target points uniform in
@@ -826,7 +850,9 @@ def wl_points(args, torch, gg, flush):
     mixed = lambda: gg.summate(*t, precision="mixed")
     t64 = _timed_events(torch, f64, args.steps, args.warmup, flush)
     tmx = _timed_events(torch, mixed, args.steps, args.warmup, flush)
+    t0 = time.perf_counter()
     ref = oracle.c_summate(gen.cov_samples, gen.z_1, gen.z_2, pos)
+    t_cpu = time.perf_counter() - t0
     got64 = f64().cpu().numpy()
     gotmx = mixed().cpu().numpy()
     s = np.sqrt(1.0 / 1000)
@@ -845,6 +871,15 @@ def wl_points(args, torch, gg, flush):
         e2e={"value": work / te2e / 1e9, "unit": UNIT,
              "h2d_bytes_per_step": int(pos.nbytes + 4 * 8 * 1000),
              "d2h_bytes_per_step": int(e2e.nbytes)},
+        cpu_baseline={"value": work / t_cpu / 1e9, "unit": UNIT,
+                      "cores": oracle.num_threads(), "kind": "port",
+                      "sample": "the whole workload (FP64 C/OpenMP oracle)"},
+        roofline={"bound": "fp32 issue",
+                  "achieved_alg_tflops": 8.0 * work / tmx / 1e12,
+                  "note": "algorithmic 2d+4 = 8 flops per mode*point plus 2 SFU "
+                          "sin/cos; the exact turn reduction issues ~20 FP32 "
+                          "operations per mode*point, and ncu measures the FMA "
+                          "pipe 64.8 % active (profiles: pointwise summary)"},
         gpu_launches=2 * args.steps)
 
 
@@ -940,6 +975,11 @@ def wl_ensemble(args, torch, gg, flush):
     t0 = time.perf_counter()
     res = bs(cov_l, z1_l, z2_l, pos, scales)
     te2e = time.perf_counter() - t0
+    import oracle
+
+    cpu = _cpu_sample(
+        lambda r: oracle.c_summate(gens[r].cov_samples, gens[r].z_1, gens[r].z_2, pos[r]),
+        list(range(len(gens))), lambda r: modes[r] * pts[r], what="realizations")
     return _line(
         args, "matern2d_ensemble512", work / t_batch / 1e9, t_batch,
         "fp32 + exact turn reduction",
@@ -963,6 +1003,7 @@ def wl_ensemble(args, torch, gg, flush):
              "h2d_bytes_per_step": int(sum(p.nbytes for p in pos)
                                        + sum(c.nbytes for c in cov_l) * 2),
              "d2h_bytes_per_step": int(sum(r.nbytes for r in res))},
+        cpu_baseline=cpu,
         gpu_launches=2 * args.steps)
 
 
@@ -1013,6 +1054,16 @@ def wl_incompr(args, torch, gg, flush):
            + (u[2, 1:-1, 1:-1, 2:] - u[2, 1:-1, 1:-1, :-2])) / 2.0
     grad_scale = ((u[0, 2:, 1:-1, 1:-1] - u[0, :-2, 1:-1, 1:-1]) / 2.0).std()
     work = nm * n ** 3
+    import oracle
+
+    g1 = np.arange(float(n))
+
+    def cpu_row(ix):
+        yz = np.array(np.meshgrid(g1, g1, indexing="ij")).reshape(2, -1)
+        row = np.concatenate([np.full((1, yz.shape[1]), float(ix)), yz])
+        oracle.c_summate_incompr(cov, z1, z2, row)
+
+    cpu = _cpu_sample(cpu_row, list(range(n)), lambda ix: nm * n * n, what="x rows")
     return _line(
         args, "gau3d_incompr_grid192_modes2000", work / ttc / 1e9, ttc,
         "f16x3 (fp32 accumulate)",
@@ -1026,6 +1077,7 @@ def wl_incompr(args, torch, gg, flush):
                        "max_abs_sigma": float(np.max(np.abs(diff_tc)))},
         divergence={"fd_rms_over_grad_rms": float(div.std() / grad_scale),
                     "note": "central differences, h=1; O(h^2) truncation"},
+        cpu_baseline=cpu,
         gpu_launches=2 * args.steps)
 
 
@@ -1085,12 +1137,21 @@ def wl_adjoint(args, torch, gg, flush):
            for name, a, b in zip(("z1", "z2", "len_scale", "anis", "angles"),
                                  grads_mixed, grads_f64)}
     work = 4000 * pts.shape[1]
+    import oracle
+
+    cov_np = data["gau3d_grad/cov"]
+    z1_np, z2_np = data["gau3d_grad/z1"], data["gau3d_grad/z2"]
+    chunks = list(range(0, pts.shape[1], 4096))
+    cpu = _cpu_sample(lambda c: oracle.c_summate(cov_np, z1_np, z2_np, pts[:, c:c + 4096]),
+                      chunks, lambda c: 4000 * min(4096, pts.shape[1] - c),
+                      what="4096-point chunks (forward summate only; a CPU gradient "
+                           "by finite differences needs two forwards per parameter)")
     return _line(
         args, "gau3d_adjoint_grid128_pts50k_modes4000", work / t_f / 1e9, t_f,
         "fp32 + exact turn reduction",
         {"points": int(pts.shape[1]), "modes": 4000, "observations": 10_000},
         fwd_ms=t_f * 1e3, fwd_bwd_ms=t_fb * 1e3, fwd_bwd_over_fwd=t_fb / t_f,
-        grad_rel_err_mixed_vs_f64=rel, gpu_launches=None)
+        grad_rel_err_mixed_vs_f64=rel, cpu_baseline=cpu, gpu_launches=None)
 
 
 def run_workload(args):
