@@ -553,8 +553,10 @@ __global__ void __launch_bounds__(kOmniThreads, 8)
         tab[c] = static_cast<short>(lo > nb ? nb : lo);
     }
     // tiles between flushes such that no 32-bit count overflows: a warp
-    // adds at most 32 x kOmniThreads pairs per field and tile
-    const int64_t per_tile = static_cast<int64_t>(32 * kOmniThreads) * (a.f_max > 1 ? a.f_max : 1);
+    // adds at most 32 x kOmniThreads pairs per field, direction and tile
+    const int64_t per_tile = static_cast<int64_t>(32 * kOmniThreads) *
+                             (a.f_max > 1 ? a.f_max : 1) *
+                             (DIRS && a.d_max > 1 ? a.d_max : 1);
     const int64_t flush_every = per_tile >= 0xffffffffLL ? 1 : 0xffffffffLL / per_tile;
     int64_t since_flush = 0;
 
