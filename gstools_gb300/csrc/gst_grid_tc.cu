@@ -75,15 +75,17 @@ __host__ __device__ constexpr int b_block_bytes(int nt) { return nt / 2 * 32; }
 // w = z1 - i z2 and put back in the epilogue).
 enum OperandKind { kOpTf32 = GST_TC_TF32, kOpF16 = GST_TC_F16 };
 
-// Modes per pipeline stage: 32 (FP16) / 16 (TF32) for 3-D grids, half that
-// for 2-D grids, whose per-CTA w*Ex slice (128 distinct x rows) is 16 times
-// larger.  A stage is 4 MMA K-steps per operand format for 3-D grids, so a
-// stage is 70 KB of shared memory either way (a 3-deep ring); measured on the
-// 256^3 workload, 32-mode FP16 stages contract 16 % faster than 16-mode ones
-// (half the barrier round trips per mode).
-__host__ __device__ constexpr int modes_per_stage(int ty, int op) {
-    return (ty == 1 ? 8 : 16) * (op == kOpF16 ? 2 : 1);
+// Modes per pipeline stage: 32 (FP16) / 16 (TF32), 4 MMA K-steps per
+// operand format, so a stage is about 70 KB of shared memory either way (a
+// 3-deep ring); measured on the 256^3 workload, 32-mode FP16 stages contract
+// 16 % faster than 16-mode ones (half the barrier round trips per mode).
+// 2-D grids (TY = 1) have A = w Ex with no y factor: the tables kernel writes
+// it pre-split in the operand layout and it is bulk-copied like B, so the
+// generator warps only drain and store (kACopied).
+__host__ __device__ constexpr int modes_per_stage(int /*ty*/, int op) {
+    return 16 * (op == kOpF16 ? 2 : 1);
 }
+__host__ __device__ constexpr bool a_copied(int ty) { return ty == 1; }
 // Modes per MMA K-step (32 bytes of K per row: 8 TF32 or 16 FP16 reals).
 __host__ __device__ constexpr int modes_per_kstep(int op) { return op == kOpF16 ? 8 : 4; }
 __host__ __device__ constexpr int ksteps_for(int ty, int op) {
@@ -453,12 +455,43 @@ __global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ mod
             re = ldexpf(fmaf(w1, c, w2 * s), -e);
             im = ldexpf(fmaf(w1, s, -w2 * c), -e);
         }
-        if (x_modes_fastest)
+        if (g.tile[1] == 1) {
+            // 2-D: the A operand itself, [Re P, -Im P] with P = w Ex, split
+            // into hi + lo in the UMMA canonical K-major layout, per
+            // 128-row block and stage [K-step][hi, lo] (the generator's
+            // layout of a slot)
+            const int kstep = mm / kMpk;
+            const uint32_t k0 = 2u * (mm % kMpk);
+            unsigned char *img = reinterpret_cast<unsigned char *>(wx) +
+                                 (blk * g.n_stages + st) *
+                                     (static_cast<int64_t>(g.ksteps) * 2 * kBlockBytes);
+            unsigned char *ah = img + (kstep * 2 + 0) * kBlockBytes;
+            unsigned char *al = img + (kstep * 2 + 1) * kBlockBytes;
+            const float vals[2] = {re, -im};
+            if constexpr (OP == kOpF16) {
+                const __half2 hi = __floats2half2_rn(vals[0], vals[1]);
+                const float2 hf = __half22float2(hi);
+                const uint32_t o = core_offset(static_cast<uint32_t>(t), k0, OP);
+                *reinterpret_cast<__half2 *>(ah + o) = hi;
+                *reinterpret_cast<__half2 *>(al + o) =
+                    __floats2half2_rn(vals[0] - hf.x, vals[1] - hf.y);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const float hi = to_tf32(vals[q]);
+                    const uint32_t o = core_offset(static_cast<uint32_t>(t), k0 + q, OP);
+                    *reinterpret_cast<float *>(ah + o) = hi;
+                    *reinterpret_cast<float *>(al + o) = vals[q] - hi;
+                }
+            }
+        } else if (x_modes_fastest) {
             wx[((blk * g.n_stages + st) * tile + t) * mps + mm] = make_float2(re, im);
-        else
+        } else {
             wx[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(re, im);
+        }
     } else if (axis == 1) {
-        ey[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(c, s);
+        if (g.tile[1] > 1)   // 2-D grids have no y table
+            ey[((blk * g.n_stages + st) * mps + mm) * tile + t] = make_float2(c, s);
     } else {
         const int cta_cols = tile / 2;
         const int bblk = b_block_bytes(tile);
@@ -518,23 +551,26 @@ struct GridArgs {
     unsigned int *err;
 };
 
-// One ring of pipeline slots per CTA: its half of B (bulk copy), its w*Ex
-// and Ey table slices (bulk copies) and its 128 rows of A (generated).
+// One ring of pipeline slots per CTA: its half of B (bulk copy) and its 128
+// rows of A: generated from the w*Ex and Ey table slices (bulk copies) on
+// 3-D grids, bulk-copied whole on 2-D grids.
 template <int TY, int OP, int NT>
 struct StageLayout {
     static constexpr int TX = kCtaRows / TY;
+    static constexpr bool kACopied = a_copied(TY);
     static constexpr int KS = ksteps_for(TY, OP);
     static constexpr int kModesPerStage = modes_per_stage(TY, OP);
     static constexpr int kChunkStages = chunk_modes(OP) / kModesPerStage;
     static constexpr int kAStageBytes = KS * 2 * kBlockBytes;
     static constexpr int kBStageBytes = KS * 2 * b_block_bytes(NT);   // per CTA
-    static constexpr int kWxBytes = kModesPerStage * TX * 8;
-    static constexpr int kEyBytes = kModesPerStage * TY * 8;
+    static constexpr int kWxBytes = kACopied ? 0 : kModesPerStage * TX * 8;
+    static constexpr int kEyBytes = kACopied ? 0 : kModesPerStage * TY * 8;
     static constexpr int kB = 0;
     static constexpr int kA = kB + kBStageBytes;
     static constexpr int kWx = kA + kAStageBytes;
     static constexpr int kEy = kWx + kWxBytes;
-    static constexpr int kCopyBytes = kBStageBytes + kWxBytes + kEyBytes;
+    static constexpr int kCopyBytes =
+        kBStageBytes + (kACopied ? kAStageBytes : kWxBytes + kEyBytes);
     static constexpr int kSlot = (kEy + kEyBytes + 1023) / 1024 * 1024;
     static constexpr int kBudget = 227 * 1024 - 2048;
     static constexpr int kPipe0 = kBudget / kSlot;
@@ -643,10 +679,18 @@ __global__ void __launch_bounds__(kThreads, 1)
                     mbar_arrive_expect_tx(&full[s], L::kCopyBytes);
                     bulk_copy_g2s(dst + L::kB, ez_src + st * 2 * kBStageBytes,
                                   kBStageBytes, &full[s]);
-                    bulk_copy_g2s(dst + L::kWx, wx_src + st * kModesPerStage * TX,
-                                  L::kWxBytes, &full[s]);
-                    bulk_copy_g2s(dst + L::kEy, ey_src + st * kModesPerStage * TY,
-                                  L::kEyBytes, &full[s]);
+                    if constexpr (L::kACopied) {
+                        // the A image of this CTA's 128 rows (2-D grids)
+                        const unsigned char *a_src =
+                            reinterpret_cast<const unsigned char *>(a.wx) +
+                            (xblk * n_all + st0 + st) * L::kAStageBytes;
+                        bulk_copy_g2s(dst + L::kA, a_src, L::kAStageBytes, &full[s]);
+                    } else {
+                        bulk_copy_g2s(dst + L::kWx, wx_src + st * kModesPerStage * TX,
+                                      L::kWxBytes, &full[s]);
+                        bulk_copy_g2s(dst + L::kEy, ey_src + st * kModesPerStage * TY,
+                                      L::kEyBytes, &full[s]);
+                    }
                 }
                 __syncwarp();
             }
@@ -799,74 +843,76 @@ __global__ void __launch_bounds__(kThreads, 1)
             // full[s] of this phase implies the slot was released (empty)
             ok = mbar_wait(&full[s], ph, a.err);
             if (__any_sync(0xffffffffu, !ok)) { ok = false; break; }
-            unsigned char *slot = smem + s * L::kSlot;
-            const float2 *swx = reinterpret_cast<const float2 *>(slot + L::kWx);
-            const float2 *sey = reinterpret_cast<const float2 *>(slot + L::kEy);
-            // This thread's modes: m0 .. m0 + kMpt - 1 of the stage, i.e.
-            // 2 kMpt consecutive reals [Re P, -Im P] of its row of A, stored
-            // in runs of kRun reals (at most one 16-byte core-matrix row).
-            constexpr int kMpt = kModesPerStage / (kGenThreads / kCtaRows);
-            constexpr int kMpk = modes_per_kstep(OP);
-            constexpr int kEps = 16 / elem_bytes(OP);    // reals per 16 bytes
-            constexpr int kRun = 2 * kMpt < kEps ? 2 * kMpt : kEps;
-            const int m0 = part * kMpt;
-#pragma unroll
-            for (int sg = 0; sg < 2 * kMpt / kRun; ++sg) {
-                const int mm = m0 + sg * kRun / 2;        // first mode of the run
-                float x[kRun];
-#pragma unroll
-                for (int m = 0; m < kRun / 2; m += 2) {
-                    float2 p0, p1;
-                    if constexpr (TY > 1) {
-                        // two modes of w*Ex per load (mode-fastest rows)
-                        const float4 p2 = *reinterpret_cast<const float4 *>(
-                            swx + xl * kModesPerStage + mm + m);
-                        p0 = make_float2(p2.x, p2.y);
-                        p1 = make_float2(p2.z, p2.w);
+            if constexpr (!L::kACopied) {
+                unsigned char *slot = smem + s * L::kSlot;
+                const float2 *swx = reinterpret_cast<const float2 *>(slot + L::kWx);
+                const float2 *sey = reinterpret_cast<const float2 *>(slot + L::kEy);
+                // This thread's modes: m0 .. m0 + kMpt - 1 of the stage, i.e.
+                // 2 kMpt consecutive reals [Re P, -Im P] of its row of A, stored
+                // in runs of kRun reals (at most one 16-byte core-matrix row).
+                constexpr int kMpt = kModesPerStage / (kGenThreads / kCtaRows);
+                constexpr int kMpk = modes_per_kstep(OP);
+                constexpr int kEps = 16 / elem_bytes(OP);    // reals per 16 bytes
+                constexpr int kRun = 2 * kMpt < kEps ? 2 * kMpt : kEps;
+                const int m0 = part * kMpt;
+    #pragma unroll
+                for (int sg = 0; sg < 2 * kMpt / kRun; ++sg) {
+                    const int mm = m0 + sg * kRun / 2;        // first mode of the run
+                    float x[kRun];
+    #pragma unroll
+                    for (int m = 0; m < kRun / 2; m += 2) {
+                        float2 p0, p1;
+                        if constexpr (TY > 1) {
+                            // two modes of w*Ex per load (mode-fastest rows)
+                            const float4 p2 = *reinterpret_cast<const float4 *>(
+                                swx + xl * kModesPerStage + mm + m);
+                            p0 = make_float2(p2.x, p2.y);
+                            p1 = make_float2(p2.z, p2.w);
+                        } else {
+                            p0 = swx[(mm + m) * TX + xl];
+                            p1 = swx[(mm + m + 1) * TX + xl];
+                        }
+                        const float2 e0 = sey[(mm + m) * TY + yl];
+                        const float2 e1 = sey[(mm + m + 1) * TY + yl];
+                        x[2 * m] = fmaf(p0.x, e0.x, -p0.y * e0.y);
+                        x[2 * m + 1] = -fmaf(p0.x, e0.y, p0.y * e0.x);
+                        x[2 * m + 2] = fmaf(p1.x, e1.x, -p1.y * e1.y);
+                        x[2 * m + 3] = -fmaf(p1.x, e1.y, p1.y * e1.x);
+                    }
+                    const int ksg = mm / kMpk;                // its K-step
+                    const uint32_t o = core_offset(row, 2u * (mm % kMpk), OP);
+                    unsigned char *ah = slot + L::kA + (ksg * 2 + 0) * kBlockBytes + o;
+                    unsigned char *al = slot + L::kA + (ksg * 2 + 1) * kBlockBytes + o;
+                    if constexpr (OP == kOpF16) {
+                        uint32_t h[kRun / 2], l[kRun / 2];
+    #pragma unroll
+                        for (int i = 0; i < kRun / 2; ++i) {
+                            const __half2 hh = __floats2half2_rn(x[2 * i], x[2 * i + 1]);
+                            const float2 hf = __half22float2(hh);
+                            h[i] = *reinterpret_cast<const uint32_t *>(&hh);
+                            l[i] = pack_f16x2(x[2 * i] - hf.x, x[2 * i + 1] - hf.y);
+                        }
+                        if constexpr (kRun == 8) {
+                            *reinterpret_cast<uint4 *>(ah) = make_uint4(h[0], h[1], h[2], h[3]);
+                            *reinterpret_cast<uint4 *>(al) = make_uint4(l[0], l[1], l[2], l[3]);
+                        } else {
+                            *reinterpret_cast<uint2 *>(ah) = make_uint2(h[0], h[1]);
+                            *reinterpret_cast<uint2 *>(al) = make_uint2(l[0], l[1]);
+                        }
                     } else {
-                        p0 = swx[(mm + m) * TX + xl];
-                        p1 = swx[(mm + m + 1) * TX + xl];
+                        static_assert(OP == kOpF16 || kRun == 4, "TF32 runs are 16 bytes");
+                        float hi[4], lo[4];
+    #pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            hi[i] = to_tf32(x[i]);
+                            lo[i] = x[i] - hi[i];   // the MMA reads lo as TF32
+                        }
+                        *reinterpret_cast<float4 *>(ah) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                        *reinterpret_cast<float4 *>(al) = make_float4(lo[0], lo[1], lo[2], lo[3]);
                     }
-                    const float2 e0 = sey[(mm + m) * TY + yl];
-                    const float2 e1 = sey[(mm + m + 1) * TY + yl];
-                    x[2 * m] = fmaf(p0.x, e0.x, -p0.y * e0.y);
-                    x[2 * m + 1] = -fmaf(p0.x, e0.y, p0.y * e0.x);
-                    x[2 * m + 2] = fmaf(p1.x, e1.x, -p1.y * e1.y);
-                    x[2 * m + 3] = -fmaf(p1.x, e1.y, p1.y * e1.x);
                 }
-                const int ksg = mm / kMpk;                // its K-step
-                const uint32_t o = core_offset(row, 2u * (mm % kMpk), OP);
-                unsigned char *ah = slot + L::kA + (ksg * 2 + 0) * kBlockBytes + o;
-                unsigned char *al = slot + L::kA + (ksg * 2 + 1) * kBlockBytes + o;
-                if constexpr (OP == kOpF16) {
-                    uint32_t h[kRun / 2], l[kRun / 2];
-#pragma unroll
-                    for (int i = 0; i < kRun / 2; ++i) {
-                        const __half2 hh = __floats2half2_rn(x[2 * i], x[2 * i + 1]);
-                        const float2 hf = __half22float2(hh);
-                        h[i] = *reinterpret_cast<const uint32_t *>(&hh);
-                        l[i] = pack_f16x2(x[2 * i] - hf.x, x[2 * i + 1] - hf.y);
-                    }
-                    if constexpr (kRun == 8) {
-                        *reinterpret_cast<uint4 *>(ah) = make_uint4(h[0], h[1], h[2], h[3]);
-                        *reinterpret_cast<uint4 *>(al) = make_uint4(l[0], l[1], l[2], l[3]);
-                    } else {
-                        *reinterpret_cast<uint2 *>(ah) = make_uint2(h[0], h[1]);
-                        *reinterpret_cast<uint2 *>(al) = make_uint2(l[0], l[1]);
-                    }
-                } else {
-                    static_assert(OP == kOpF16 || kRun == 4, "TF32 runs are 16 bytes");
-                    float hi[4], lo[4];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        hi[i] = to_tf32(x[i]);
-                        lo[i] = x[i] - hi[i];   // the MMA reads lo as TF32
-                    }
-                    *reinterpret_cast<float4 *>(ah) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-                    *reinterpret_cast<float4 *>(al) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-                }
+                fence_async_smem();
             }
-            fence_async_smem();
             __syncwarp();
             if (lane == 0) mbar_arrive(rank == 0 ? &ready[s] : &gen_done[s]);
             // Drain a finished chunk as soon as the tensor cores are done
@@ -1126,10 +1172,16 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
     if (2 * p.pair_blocks[0] * p.pair_blocks[1] * p.pair_blocks[2] > 0x7fffffffLL)
         return GST_ERR_TOO_LARGE;
     const size_t per_stage = mps * sizeof(float2);
-    const size_t wx_bytes = static_cast<size_t>(g.blocks[0]) * g.n_stages *
-                            per_stage * g.tile[0];
-    const size_t ey_bytes = static_cast<size_t>(g.blocks[1]) * g.n_stages *
-                            per_stage * g.tile[1];
+    // 2-D: the pre-split A image (per 128-row block and stage) instead of
+    // the w*Ex table, and no y table
+    const size_t wx_bytes =
+        a_copied(p.ty) ? static_cast<size_t>(g.blocks[0]) * g.n_stages * g.ksteps * 2 *
+                             kBlockBytes
+                       : static_cast<size_t>(g.blocks[0]) * g.n_stages * per_stage *
+                             g.tile[0];
+    const size_t ey_bytes = a_copied(p.ty) ? 0
+                                           : static_cast<size_t>(g.blocks[1]) *
+                                                 g.n_stages * per_stage * g.tile[1];
     const size_t ez_bytes = static_cast<size_t>(g.blocks[2]) * g.n_stages * 2 *
                             g.ksteps * 2 * b_block_bytes(g.tile[2]);
     p.pt_base1 = g.blocks[0] * g.tile[0];
