@@ -321,12 +321,15 @@ __device__ __forceinline__ T pick3(const T (&v)[3], int i) {
     return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]);
 }
 
-// Per-mode and per-point splits for the table kernel, so that it runs in
-// FP32 only (GB300's FP64 rate is 1/64 of FP32).  Mode entry (8 floats):
-// qh[3], ql[3] of q = k / (2 pi) (12-bit head + tail, see gst_mixed.cuh) and
-// the weighted amplitudes f z1, f z2.  Point entry: xh, xl, xf, 0.
+// Per-mode and per-point inputs of the table kernel.  Mode entry: q = k /
+// (2 pi) per axis in FP64 and the weighted amplitudes f z1, f z2.  Point
+// entry: the FP64 coordinate.  The tables are O((nx + ny + nz) N) work, so
+// their phase q x is formed and reduced to [-1/2, 1/2] turns in FP64 (exact
+// reduction, any domain size); only the sincospi of the reduced phase is
+// FP32.
 struct ModeSplit {
-    float qh[3], ql[3], w1, w2;
+    double q[3];
+    float w1, w2;
 };
 
 __global__ void grid_prep_kernel(GridGeom g, const double *__restrict__ cov,
@@ -336,7 +339,7 @@ __global__ void grid_prep_kernel(GridGeom g, const double *__restrict__ cov,
                                  int64_t n_pad_modes, int64_t pt_base1,
                                  int64_t pt_base2, int64_t n_pt_total,
                                  ModeSplit *__restrict__ modes,
-                                 float4 *__restrict__ points,
+                                 double *__restrict__ points,
                                  unsigned int *__restrict__ amp_max) {
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i < n_pad_modes) {
@@ -357,9 +360,7 @@ __global__ void grid_prep_kernel(GridGeom g, const double *__restrict__ cov,
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const int src = g.src[a];
-                const double q = src >= 0 ? cov[src * g.n_modes + i] * kInv2Pi : 0.0;
-                m.qh[a] = split_hi12(q);
-                m.ql[a] = static_cast<float>(q - static_cast<double>(m.qh[a]));
+                m.q[a] = src >= 0 ? cov[src * g.n_modes + i] * kInv2Pi : 0.0;
             }
             m.w1 = static_cast<float>(f * z1[i]);
             m.w2 = static_cast<float>(f * z2[i]);
@@ -376,9 +377,7 @@ __global__ void grid_prep_kernel(GridGeom g, const double *__restrict__ cov,
     double x = 0.0;
     if (r < pick3(g.n, axis) && pick3(g.src, axis) >= 0)
         x = axes[pick3(g.off, axis) + r];
-    const float xh = split_hi12(x);
-    points[p] = make_float4(xh, static_cast<float>(x - static_cast<double>(xh)),
-                            static_cast<float>(x), 0.0f);
+    points[p] = x;
 }
 
 // 2^-e with amp = m 2^e, m in [0.5, 1): scales the amplitudes below 1.
@@ -388,17 +387,17 @@ __device__ __forceinline__ int amp_exponent(const unsigned int *amp_max) {
     return e;
 }
 
-// One thread per (axis point, mode), points fastest, FP32 only.  Axis x
+// One thread per (axis point, mode), points fastest.  Axis x
 // writes w*Ex * 2^-e (amplitudes normalised below 1), axis y writes Ey
 // (complex FP32, blocked [block][stage][mode][tile]); axis z writes the
 // pre-split image of [Re Ez, Im Ez] in the operand format: per NT-point
 // block and stage, the half of each CTA of a pair (NT / 2 points) is one
 // contiguous run of [K-step][hi, lo] blocks in the UMMA canonical K-major
-// layout.  The phase is reduced to turns exactly (gst_mixed.cuh) before the
-// FP32 sincospi.
+// layout.  The phase q x is formed and reduced to [-1/2, 1/2] turns in FP64
+// before the FP32 sincospi.
 template <int OP>
 __global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ modes,
-                                   const float4 *__restrict__ points,
+                                   const double *__restrict__ points,
                                    int64_t pt_base1, int64_t pt_base2,
                                    const unsigned int *__restrict__ amp_max,
                                    float2 *__restrict__ wx, float2 *__restrict__ ey,
@@ -431,17 +430,13 @@ __global__ void grid_tables_kernel(GridGeom g, const ModeSplit *__restrict__ mod
 
     float c = 0.0f, s = 0.0f;
     const bool live = (j < g.n_modes) && (r < pick3(g.n, axis));
-    const float *mf = reinterpret_cast<const float *>(modes + j);
-    const float w1 = mf[6], w2 = mf[7];
+    const ModeSplit &md = modes[j];
+    const float w1 = md.w1, w2 = md.w2;
     if (live) {
-        const float4 pt = points[(axis == 0 ? 0 : (axis == 1 ? pt_base1 : pt_base2)) + r];
-        MixedPoint<1> mp;
-        mp.xh[0] = pt.x;
-        mp.xl[0] = pt.y;
-        mp.xf[0] = pt.z;
-        const float qh[3] = {mf[axis], 0.0f, 0.0f};
-        const float ql[3] = {mf[3 + axis], 0.0f, 0.0f};
-        sincospif(2.0f * mixed_turns<1>(qh, ql, mp), &s, &c);
+        const double x = points[(axis == 0 ? 0 : (axis == 1 ? pt_base1 : pt_base2)) + r];
+        const double t = pick3(md.q, axis) * x;            // turns
+        const float rt = static_cast<float>(t - rint(t));  // exact, in [-1/2, 1/2]
+        sincospif(2.0f * rt, &s, &c);
     }
     const int64_t st = j / mps;
     const int mm = static_cast<int>(j % mps);
@@ -1192,7 +1187,7 @@ int make_plan(int dim, int64_t n_modes, const int64_t *axis_len, GridPlan &p,
     p.ey_off = align_up(p.wx_off + wx_bytes, 256);
     p.modes_off = align_up(p.ey_off + ey_bytes, 256);
     p.points_off = align_up(p.modes_off + sizeof(ModeSplit) * g.n_stages * mps, 256);
-    p.amp_off = align_up(p.points_off + sizeof(float4) * p.n_pt_total, 256);
+    p.amp_off = align_up(p.points_off + sizeof(double) * p.n_pt_total, 256);
     p.total = p.amp_off + sizeof(unsigned int);
     return GST_OK;
 }
@@ -1203,7 +1198,7 @@ int run_tables(const GridPlan &p, const double *axes, const double *cov,
     const GridGeom &g = p.g;
     const int64_t n_pad_modes = g.n_stages * modes_per_stage(p.ty, g.op);
     ModeSplit *modes = reinterpret_cast<ModeSplit *>(ws + p.modes_off);
-    float4 *points = reinterpret_cast<float4 *>(ws + p.points_off);
+    double *points = reinterpret_cast<double *>(ws + p.points_off);
     unsigned int *amp = reinterpret_cast<unsigned int *>(ws + p.amp_off);
     const int threads = 256;
     GST_TRY_CUDA(cudaMemsetAsync(amp, 0, sizeof(unsigned int), s));

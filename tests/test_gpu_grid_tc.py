@@ -88,6 +88,27 @@ def test_tc_tile_widths(cuda_lib, nz, nt, dim):
         assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (out_dtype, rms, mx)
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_tc_far_from_origin(cuda_lib, dim):
+    """Axes 1e5 - 3e5 from the origin with heavy-tailed wave numbers: per-axis
+    phases up to ~6e5 turns, reduced exactly (FP64) in the tables before the
+    FP32 sincospi."""
+    n_modes = 300
+    cov, z1, z2 = case(7 * dim, dim, n_modes, k_scale=1.0)
+    axes = [1.0e5 + np.arange(40.0) * 0.37, 2.0e5 - np.arange(30.0) * 0.51,
+            -3.0e5 + np.arange(36.0) * 0.29][:dim]
+    got = gg.summate_grid(cov, z1, z2, axes, precision="mixed", method="tensor")
+    ref = grid_ref(cov, z1, z2, axes)
+    rms, mx = errors(got, ref, n_modes)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (rms, mx)
+    # the mixed pointwise kernel reduces each phase in FP32 splits (error
+    # about |t| 2^-35 turns): within its domain, phases up to ~1e5 turns
+    near = [a - a[0] + a[0] / 6.0 for a in axes]
+    got_pw = gg.summate_grid(cov, z1, z2, near, precision="mixed", method="pointwise")
+    rms, mx = errors(got_pw, grid_ref(cov, z1, z2, near), n_modes)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, ("pointwise", rms, mx)
+
+
 def test_tc_exp3d_workload_slab(cuda_lib, workloads):
     """The benchmark's modes (3-D anisotropic Exponential, 2000 modes) on a
     full 256^3 grid, checked against the oracle on scattered slabs."""
