@@ -644,10 +644,12 @@ def _line(args, workload, value, t_step, dtype, config, **extra):
     return line
 
 
-def _cpu_sample(fn, items, work_of, target_s=5.0, what="items"):
+def _cpu_sample(fn, items, work_of, target_s=5.0, what="items", skip=False):
     """Time the oracle (all host cores) on the first items of a workload,
     growing the sample until it runs about target_s seconds or covers every
     item; returns a cpu_baseline dict in G mode*point/s."""
+    if skip:
+        return None
     import oracle
 
     oracle.build()
@@ -979,7 +981,8 @@ def wl_ensemble(args, torch, gg, flush):
 
     cpu = _cpu_sample(
         lambda r: oracle.c_summate(gens[r].cov_samples, gens[r].z_1, gens[r].z_2, pos[r]),
-        list(range(len(gens))), lambda r: modes[r] * pts[r], what="realizations")
+        list(range(len(gens))), lambda r: modes[r] * pts[r], what="realizations",
+        skip=args.no_cpu_baseline)
     return _line(
         args, "matern2d_ensemble512", work / t_batch / 1e9, t_batch,
         "fp32 + exact turn reduction",
@@ -1063,7 +1066,8 @@ def wl_incompr(args, torch, gg, flush):
         row = np.concatenate([np.full((1, yz.shape[1]), float(ix)), yz])
         oracle.c_summate_incompr(cov, z1, z2, row)
 
-    cpu = _cpu_sample(cpu_row, list(range(n)), lambda ix: nm * n * n, what="x rows")
+    cpu = _cpu_sample(cpu_row, list(range(n)), lambda ix: nm * n * n, what="x rows",
+                      skip=args.no_cpu_baseline)
     return _line(
         args, "gau3d_incompr_grid192_modes2000", work / ttc / 1e9, ttc,
         "f16x3 (fp32 accumulate)",
@@ -1145,7 +1149,8 @@ def wl_adjoint(args, torch, gg, flush):
     cpu = _cpu_sample(lambda c: oracle.c_summate(cov_np, z1_np, z2_np, pts[:, c:c + 4096]),
                       chunks, lambda c: 4000 * min(4096, pts.shape[1] - c),
                       what="4096-point chunks (forward summate only; a CPU gradient "
-                           "by finite differences needs two forwards per parameter)")
+                           "by finite differences needs two forwards per parameter)",
+                      skip=args.no_cpu_baseline)
     return _line(
         args, "gau3d_adjoint_grid128_pts50k_modes4000", work / t_f / 1e9, t_f,
         "fp32 + exact turn reduction",

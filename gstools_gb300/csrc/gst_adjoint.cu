@@ -73,12 +73,17 @@ __global__ void __launch_bounds__(kThreads) vjp_modes_kernel(const VjpArgs a) {
 
     const int64_t p_begin = static_cast<int64_t>(blockIdx.y) * a.pts_per_split;
     const int64_t p_end = min(p_begin + a.pts_per_split, a.n_pts);
+    // mixed: positions relative to the first point (the finish kernel
+    // rotates the sums back, gst_mixed.cuh)
+    double x0[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) x0[d] = PREC == kMixed ? origin_coord(a.pos + d * a.n_pts) : 0.0;
     for (int64_t c0 = p_begin; c0 < p_end; c0 += kChunk) {
         const int64_t i = c0 + tid;
         const bool in = i < p_end;
         double xv[DIM];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) xv[d] = in ? a.pos[d * a.n_pts + i] : 0.0;
+        for (int d = 0; d < DIM; ++d) xv[d] = in ? a.pos[d * a.n_pts + i] - x0[d] : 0.0;
         const double gv = in ? a.g[i] : 0.0;  // g = 0 pads the chunk
         if (PREC == kF64) {
 #pragma unroll
@@ -164,12 +169,18 @@ __global__ void __launch_bounds__(kThreads) vjp_modes_kernel(const VjpArgs a) {
     }
 }
 
-// Sums the slices in order and forms the gradients.
+// Sums the slices in order and forms the gradients.  With `shifted` (mixed
+// path) the sums ran over phases <k, x - x0> and positions x - x0, x0 the
+// first point; with a = <k, x0>:
+//   C  = cos(a) C' - sin(a) S',     S  = sin(a) C' + cos(a) S',
+//   Cx = x0 C + cos(a) C'x - sin(a) S'x,   Sx = x0 S + sin(a) C'x + cos(a) S'x.
 __global__ void vjp_modes_finish_kernel(int dim, int64_t n_modes, int64_t n_split,
                                         const double *__restrict__ partial,
                                         const double *__restrict__ z1,
                                         const double *__restrict__ z2,
-                                        double *grad_z1, double *grad_z2,
+                                        const double *__restrict__ cov,
+                                        const double *__restrict__ pos, int64_t n_pts,
+                                        int shifted, double *grad_z1, double *grad_z2,
                                         double *grad_cov) {
     const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (j >= n_modes) return;
@@ -178,6 +189,31 @@ __global__ void vjp_modes_finish_kernel(int dim, int64_t n_modes, int64_t n_spli
     for (int64_t k = 0; k < n_split; ++k) {
         const double *src = partial + (k * n_modes + j) * na;
         for (int c = 0; c < na; ++c) s[c] += src[c];
+    }
+    if (shifted) {
+        double k[4] = {0.0, 0.0, 0.0, 0.0}, x0[3] = {0.0, 0.0, 0.0};
+        for (int d = 0; d < dim; ++d) {
+            k[d] = cov[d * n_modes + j];
+            x0[d] = origin_coord(pos + d * n_pts);
+        }
+        double ca = 1.0, sa = 0.0;   // (cos a, sin a) from rotating (1, 0)
+        double one = 1.0, zero = 0.0;
+        rotate_to_origin(k, dim, x0, one, zero);   // (cos a, -sin a)
+        ca = one;
+        sa = -zero;
+        const double c = ca * s[0] - sa * s[1];
+        const double sn = sa * s[0] + ca * s[1];
+        double t[8];
+        for (int d = 0; d < dim; ++d) {
+            t[2 + d] = x0[d] * c + ca * s[2 + d] - sa * s[2 + dim + d];
+            t[2 + dim + d] = x0[d] * sn + sa * s[2 + d] + ca * s[2 + dim + d];
+        }
+        s[0] = c;
+        s[1] = sn;
+        for (int d = 0; d < dim; ++d) {
+            s[2 + d] = t[2 + d];
+            s[2 + dim + d] = t[2 + dim + d];
+        }
     }
     if (grad_z1) grad_z1[j] = s[0];
     if (grad_z2) grad_z2[j] = s[1];
@@ -231,7 +267,8 @@ int run_vjp_modes(int prec, int dim, int64_t n_modes, int64_t n_pts,
     GST_TRY_CUDA(prec == kF64 ? launch_vjp<kF64>(dim, grid, args, s)
                               : launch_vjp<kMixed>(dim, grid, args, s));
     vjp_modes_finish_kernel<<<static_cast<unsigned>(ceil_div(n_modes, 256)), 256, 0, s>>>(
-        dim, n_modes, n_split, args.partial, z1, z2, grad_z1, grad_z2, grad_cov);
+        dim, n_modes, n_split, args.partial, z1, z2, cov, pos, n_pts,
+        prec == kMixed ? 1 : 0, grad_z1, grad_z2, grad_cov);
     GST_TRY_CUDA(cudaGetLastError());
     return GST_OK;
 }

@@ -57,13 +57,13 @@ struct Tile {
 };
 
 struct Layout {
-    size_t counter_off, items_off, tiles_off, table_off, total;
+    size_t counter_off, items_off, tiles_off, table_off, shift_off, total;
     int64_t n_tiles, table_entries;
 };
 
 int points_per_tile(int variant) { return kThreads * (variant == 0 ? 2 : 4); }
 
-int make_layout(int64_t n_items, const int64_t *modes, const int64_t *pts,
+int make_layout(int dim, int64_t n_items, const int64_t *modes, const int64_t *pts,
                 int variant, Layout &l) {
     if (n_items < 0 || (n_items > 0 && (modes == nullptr || pts == nullptr)))
         return GST_ERR_INVALID_ARGUMENT;
@@ -81,19 +81,38 @@ int make_layout(int64_t n_items, const int64_t *modes, const int64_t *pts,
     l.items_off = 256;
     l.tiles_off = align_up(l.items_off + sizeof(Item) * n_items, 256);
     l.table_off = align_up(l.tiles_off + sizeof(Tile) * l.n_tiles, 256);
-    l.total = l.table_off + static_cast<size_t>(l.table_entries) * kEntryBytes;
+    // positions relative to each realization's first point (mixed path)
+    int64_t total_pts = 0;
+    for (int64_t r = 0; r < n_items; ++r) total_pts += pts[r];
+    l.shift_off = align_up(l.table_off + static_cast<size_t>(l.table_entries) * kEntryBytes,
+                           256);
+    l.total = l.shift_off + sizeof(double) * static_cast<size_t>(dim > 0 ? dim : 0) *
+                                static_cast<size_t>(total_pts);
     return GST_OK;
 }
 
-// One thread per table entry of realization blockIdx.y.
+// Coordinate d of realization it's shift origin: its first point
+// (gst_mixed.cuh, rotate_to_origin).
+__device__ __forceinline__ double item_origin(const double *pos, int64_t total_pts,
+                                              const Item &it, int d, int dim) {
+    return (d < dim && it.n_pts > 0) ? origin_coord(pos + d * total_pts + it.pt_off)
+                                     : 0.0;
+}
+
+// One thread per table entry of realization blockIdx.y; amplitudes rotated
+// to the realization's first point.
 __global__ void pack_batch_kernel(int dim, const Item *__restrict__ items,
                                   int64_t total_modes,
                                   const double *__restrict__ cov,
                                   const double *__restrict__ z1,
                                   const double *__restrict__ z2,
+                                  const double *__restrict__ pos, int64_t total_pts,
                                   unsigned char *__restrict__ table) {
     const Item it = items[blockIdx.y];
     const int64_t padded = padded_modes(it.n_modes);
+    const double x0[3] = {item_origin(pos, total_pts, it, 0, dim),
+                          item_origin(pos, total_pts, it, 1, dim),
+                          item_origin(pos, total_pts, it, 2, dim)};
     for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
          j < padded; j += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         double k[4] = {0.0, 0.0, 0.0, 0.0};
@@ -103,9 +122,28 @@ __global__ void pack_batch_kernel(int dim, const Item *__restrict__ items,
             for (int d = 0; d < dim; ++d) k[d] = cov[d * total_modes + it.mode_off + j];
             a1 = z1[it.mode_off + j];
             a2 = z2[it.mode_off + j];
+            rotate_to_origin(k, dim, x0, a1, a2);
         }
         mixed_pack_entry(reinterpret_cast<float *>(table) + (it.table_off + j) * 16,
                          k, a1, a2, proj);
+    }
+}
+
+// Positions relative to each realization's first point, into the
+// workspace: realization blockIdx.y, grid-stride over its points.  (Done
+// here rather than at the kernel's point loads, where the extra operands
+// were measured to cost the summation 3.7 %.)
+__global__ void shift_points_kernel(int dim, const Item *__restrict__ items,
+                                    const double *__restrict__ pos, int64_t total_pts,
+                                    double *__restrict__ shifted) {
+    const Item it = items[blockIdx.y];
+    for (int d = 0; d < dim; ++d) {
+        const double x0 = item_origin(pos, total_pts, it, d, dim);
+        const double *src = pos + d * total_pts + it.pt_off;
+        double *dst = shifted + d * total_pts + it.pt_off;
+        for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+             i < it.n_pts; i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+            dst[i] = src[i] - x0;
     }
 }
 
@@ -243,7 +281,7 @@ int gst_batch_workspace_size(int dim, int64_t n_items, const int64_t *mode_count
     if (bytes == nullptr) return GST_ERR_INVALID_ARGUMENT;
     if (dim < 1 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
     gst::Layout l;
-    const int rc = gst::make_layout(n_items, mode_counts, point_counts, variant, l);
+    const int rc = gst::make_layout(dim, n_items, mode_counts, point_counts, variant, l);
     if (rc) return rc;
     *bytes = l.total;
     return GST_OK;
@@ -255,7 +293,7 @@ int gst_batch_prepare(int dim, int64_t n_items, const int64_t *mode_counts,
     using namespace gst;
     if (dim < 1 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
     Layout l;
-    int rc = make_layout(n_items, mode_counts, point_counts, variant, l);
+    int rc = make_layout(dim, n_items, mode_counts, point_counts, variant, l);
     if (rc) return rc;
     if (workspace == nullptr || workspace_bytes < l.total) return GST_ERR_INVALID_ARGUMENT;
     if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0) return GST_ERR_ALIGNMENT;
@@ -305,7 +343,7 @@ int gst_batch_run(int dim, int64_t n_items, const int64_t *mode_counts,
     if (out_type != GST_OUT_F64 && out_type != GST_OUT_F32)
         return GST_ERR_INVALID_ARGUMENT;
     Layout l;
-    int rc = make_layout(n_items, mode_counts, point_counts, variant, l);
+    int rc = make_layout(dim, n_items, mode_counts, point_counts, variant, l);
     if (rc) return rc;
     int64_t total_modes = 0, total_pts = 0, max_padded = 0;
     for (int64_t r = 0; r < n_items; ++r) {
@@ -333,7 +371,18 @@ int gst_batch_run(int dim, int64_t n_items, const int64_t *mode_counts,
                         static_cast<unsigned>(n_items));
         pack_batch_kernel<<<grid, 256, 0, s>>>(
             dim, reinterpret_cast<const Item *>(ws + l.items_off), total_modes, cov,
-            z_1, z_2, ws + l.table_off);
+            z_1, z_2, pos, total_pts, ws + l.table_off);
+        GST_TRY_CUDA(cudaGetLastError());
+    }
+    double *shifted = reinterpret_cast<double *>(ws + l.shift_off);
+    {
+        int64_t max_pts = 0;
+        for (int64_t r = 0; r < n_items; ++r) max_pts = std::max(max_pts, point_counts[r]);
+        const dim3 grid(static_cast<unsigned>(std::max<int64_t>(
+                            1, std::min<int64_t>(ceil_div(max_pts, 256), 64))),
+                        static_cast<unsigned>(n_items));
+        shift_points_kernel<<<grid, 256, 0, s>>>(
+            dim, reinterpret_cast<const Item *>(ws + l.items_off), pos, total_pts, shifted);
         GST_TRY_CUDA(cudaGetLastError());
     }
     BatchArgs args{};
@@ -342,7 +391,7 @@ int gst_batch_run(int dim, int64_t n_items, const int64_t *mode_counts,
     args.n_tiles = l.n_tiles;
     args.counter = reinterpret_cast<unsigned int *>(ws + l.counter_off);
     args.table = ws + l.table_off;
-    args.pos = pos;
+    args.pos = shifted;
     args.total_pts = total_pts;
     args.scales = scales;
     args.out = out;

@@ -64,6 +64,38 @@ __device__ __forceinline__ void mixed_sincos(const float (&qh)[3],
     __sincosf(mixed_turns<DIM>(qh, ql, p) * kTwoPiF, sn, cs);
 }
 
+// Origin shift of the mixed paths: with x = x0 + x' and theta = <k, x>,
+//   a1 cos(theta) + a2 sin(theta) = a1' cos(<k, x'>) + a2' sin(<k, x'>),
+//   a1' = a1 cos(a) + a2 sin(a),  a2' = a2 cos(a) - a1 sin(a),  a = <k, x0>,
+// so the per-point phases span only the extent of the points around x0 (the
+// split turn reduction's error grows with |<k, x>|).  The rotation is formed
+// once per mode: <k, x0> / 2 pi reduced exactly in FP64, the sincospi of the
+// reduced angle in FP32.  A coordinate of x0 that is not finite is taken as 0.
+__device__ __forceinline__ double origin_coord(const double *p) {
+    if (p == nullptr) return 0.0;
+    const double v = *p;
+    return isfinite(v) ? v : 0.0;
+}
+
+__device__ __forceinline__ void rotate_to_origin(const double (&k)[4], int dim,
+                                                 const double (&x0)[3], double &a1,
+                                                 double &a2) {
+    constexpr double kInv2PiD = 0.15915494309189533576888376337251436;
+    double t = 0.0;
+    for (int d = 0; d < dim && d < 3; ++d) t += (k[d] * kInv2PiD) * x0[d];
+    const double r = t - rint(t);   // exact, |r| <= 1/2
+    // FP32 sincospi of the reduced angle: the rotated amplitudes are rounded
+    // to FP32 in the table anyway (an FP64 sincospi per mode was measured to
+    // add 1.5 % to a 1000-mode x 100 000-point call)
+    float sf, cf;
+    sincospif(2.0f * static_cast<float>(r), &sf, &cf);
+    const double s = sf, c = cf;
+    const double b1 = a1 * c + a2 * s;
+    const double b2 = a2 * c - a1 * s;
+    a1 = b1;
+    a2 = b2;
+}
+
 // Packs one mode into the 16-float mixed table entry
 //   qh0 qh1 qh2 a1 | ql0 ql1 ql2 a2 | p0 p1 p2 0 | 0 0 0 0
 __device__ __forceinline__ void mixed_pack_entry(float *e, const double (&k)[4],

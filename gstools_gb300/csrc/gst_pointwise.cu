@@ -83,7 +83,8 @@ __global__ void pack_modes_kernel(int dim, int64_t n_modes, int64_t n_padded,
                                   const double *__restrict__ z1,
                                   const double *__restrict__ z2,
                                   const double *__restrict__ weight,
-                                  void *__restrict__ table) {
+                                  const double *o0, const double *o1,
+                                  const double *o2, void *__restrict__ table) {
     const int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (j >= n_padded) return;
     double k[4] = {0.0, 0.0, 0.0, 0.0};
@@ -124,8 +125,11 @@ __global__ void pack_modes_kernel(int dim, int64_t n_modes, int64_t n_padded,
             for (int d = 0; d < 3; ++d) e[5 + d] = proj[d];
         }
     } else {
-        mixed_pack_entry(static_cast<float *>(table) + j * 16, k, a1 * w, a2 * w,
-                         proj);
+        // amplitudes rotated to the points' origin (gst_mixed.cuh)
+        double b1 = a1 * w, b2 = a2 * w;
+        const double x0[3] = {origin_coord(o0), origin_coord(o1), origin_coord(o2)};
+        if (j < n_modes) rotate_to_origin(k, dim, x0, b1, b2);
+        mixed_pack_entry(static_cast<float *>(table) + j * 16, k, b1, b2, proj);
     }
 }
 
@@ -138,6 +142,7 @@ struct PointwiseArgs {
     int64_t n_pts;
     const double *pos;           // (dim, n_pts) for unstructured points
     const double *axes;          // concatenated axis arrays (structured)
+    const double *origin[3];     // mixed: coordinates of the shift origin
     int64_t axis_len[4];
     int64_t axis_off[4];
     void *out;                   // final output, or FP64 partials
@@ -200,11 +205,19 @@ __global__ void __launch_bounds__(Tiling<PREC>::kThreads,
         }
     }
 
-    // Mixed precision: positions split once per point.
+    // Mixed precision: positions relative to the origin the mode table was
+    // rotated to, split once per point.
     MixedPoint<DIM> mp[P];
     if (PREC == kMixed) {
+        double x0[DIM];
 #pragma unroll
-        for (int p = 0; p < P; ++p) mp[p] = mixed_split_point<DIM>(x[p]);
+        for (int d = 0; d < DIM; ++d) x0[d] = origin_coord(a.origin[d]);
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) x[p][d] -= x0[d];
+            mp[p] = mixed_split_point<DIM>(x[p]);
+        }
     }
 
     double acc[P][NC];
@@ -405,14 +418,34 @@ cudaError_t dispatch(int pos_mode, int dim, dim3 grid, const PointwiseArgs &args
     return dispatch_dim<KIND, PREC, kUnstructured>(dim, grid, args, s);
 }
 
+// Device addresses of the coordinates of the mixed paths' shift origin: the
+// first point (unstructured) or the first value of each axis (structured).
+void origin_ptrs(const Request &r, const double *(&o)[3]) {
+    int64_t off = 0;
+    for (int d = 0; d < 3; ++d) {
+        o[d] = nullptr;
+        if (d >= r.dim || r.n_pts == 0) continue;
+        if (r.pos_mode == kUnstructured) {
+            o[d] = r.pos + d * r.n_pts;
+        } else {
+            o[d] = r.axes + off;
+            off += r.axis_len[d];
+        }
+    }
+}
+
 template <int KIND, int PREC>
 void pack(const Request &r, int64_t n_padded, void *table) {
-    const int threads = 256;
+    // small blocks: the mixed entries' FP64 origin rotation is FP64-pipe
+    // work, spread over many SMs (256-thread blocks put 1000 modes on 4 SMs)
+    const int threads = 64;
     const int64_t blocks = ceil_div(n_padded, threads);
+    const double *o[3];
+    origin_ptrs(r, o);
     pack_modes_kernel<KIND, PREC><<<static_cast<unsigned>(blocks), threads, 0,
                                     r.stream>>>(r.dim, r.n_modes, n_padded,
                                                 r.cov, r.z1, r.z2, r.weight,
-                                                table);
+                                                o[0], o[1], o[2], table);
 }
 
 int run(const Request &r) {
@@ -504,6 +537,7 @@ int run(const Request &r) {
     args.n_pts = r.n_pts;
     args.pos = r.pos;
     args.axes = r.axes;
+    origin_ptrs(r, args.origin);
     int64_t off = 0;
     for (int d = 0; d < 4; ++d) {
         args.axis_len[d] = d < r.dim ? r.axis_len[d] : 1;

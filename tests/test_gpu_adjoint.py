@@ -52,6 +52,24 @@ def test_vjp_matches_torch_autograd(cuda_lib, dim, precision, tol):
         assert rel(t.grad, r) <= tol, (name, rel(t.grad, r))
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_vjp_mixed_far_from_origin(cuda_lib, dim):
+    """Points 2e5 from the origin: the mixed adjoint sums run relative to the
+    first point and are rotated back per mode; gradients match the FP64
+    adjoint (cov gradients scale with |x|, so compared on their own norm)."""
+    cov, z1, z2, pos, w = leaves(10 + dim, dim, 300, 2000)
+    with torch.no_grad():
+        pos += 2.0e5
+    grads = {}
+    for prec in ("f64", "mixed"):
+        for t in (cov, z1, z2, pos):
+            t.grad = None
+        (summate_torch(cov, z1, z2, pos, prec) * w).sum().backward()
+        grads[prec] = [t.grad.clone() for t in (cov, z1, z2, pos)]
+    for name, a, b in zip(("cov", "z1", "z2", "pos"), grads["mixed"], grads["f64"]):
+        assert rel(a, b) <= 1e-4, (name, rel(a, b))
+
+
 def test_vjp_workload_modes(cuda_lib, workloads):
     """4000 modes of the 3-D Gaussian (reference RNG) at 2048 points."""
     c = workloads.case("gau3d_grad")

@@ -56,6 +56,20 @@ def test_batched_matches_oracle(cuda_lib, dim):
     assert bs.variant in gg.batched.VARIANTS
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_batched_far_from_origin(cuda_lib, dim):
+    """Point sets 1e5 - 1e6 from the origin (phases up to ~1e6 turns): each
+    realization's phases are taken relative to its first point."""
+    modes, pts, cov, z1, z2, pos, var = ensemble(40 + dim, dim, 9, zero_item=False)
+    rng = np.random.RandomState(dim)
+    pos = [p + rng.uniform(1e5, 1e6, size=(dim, 1)) for p in pos]
+    cov = [c * 8.0 for c in cov]
+    scales = np.sqrt(var / np.maximum(modes, 1))
+    bs = gg.BatchedSummator(dim, modes, pts, out_dtype="float64")
+    fields = bs(cov, z1, z2, pos, scales)
+    check(fields, modes, cov, z1, z2, pos, var)
+
+
 def test_graph_replay_with_new_data(cuda_lib):
     modes, pts, cov, z1, z2, pos, var = ensemble(7, 2, 17)
     scales = np.sqrt(var / np.maximum(modes, 1))

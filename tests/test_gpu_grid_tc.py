@@ -91,8 +91,8 @@ def test_tc_tile_widths(cuda_lib, nz, nt, dim):
 @pytest.mark.parametrize("dim", [2, 3])
 def test_tc_far_from_origin(cuda_lib, dim):
     """Axes 1e5 - 3e5 from the origin with heavy-tailed wave numbers: per-axis
-    phases up to ~6e5 turns, reduced exactly (FP64) in the tables before the
-    FP32 sincospi."""
+    phases up to ~6e5 turns.  Tensor cores: reduced exactly (FP64) in the
+    tables; mixed pointwise: relative to the first point."""
     n_modes = 300
     cov, z1, z2 = case(7 * dim, dim, n_modes, k_scale=1.0)
     axes = [1.0e5 + np.arange(40.0) * 0.37, 2.0e5 - np.arange(30.0) * 0.51,
@@ -101,12 +101,17 @@ def test_tc_far_from_origin(cuda_lib, dim):
     ref = grid_ref(cov, z1, z2, axes)
     rms, mx = errors(got, ref, n_modes)
     assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, (rms, mx)
-    # the mixed pointwise kernel reduces each phase in FP32 splits (error
-    # about |t| 2^-35 turns): within its domain, phases up to ~1e5 turns
-    near = [a - a[0] + a[0] / 6.0 for a in axes]
-    got_pw = gg.summate_grid(cov, z1, z2, near, precision="mixed", method="pointwise")
-    rms, mx = errors(got_pw, grid_ref(cov, z1, z2, near), n_modes)
+    # the mixed pointwise kernel: phases relative to the grid's first point
+    # (amplitudes rotated per mode), so only the grid's extent enters the
+    # FP32 split reduction
+    got_pw = gg.summate_grid(cov, z1, z2, axes, precision="mixed", method="pointwise")
+    rms, mx = errors(got_pw, ref, n_modes)
     assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, ("pointwise", rms, mx)
+    # and on the same points as an unstructured set
+    pts = np.array(np.meshgrid(*axes, indexing="ij")).reshape(dim, -1)
+    got_u = gg.summate(cov, z1, z2, pts[:, ::-1].copy(), precision="mixed")
+    rms, mx = errors(got_u[::-1].reshape(ref.shape), ref, n_modes)
+    assert rms <= RMS_SIGMA and mx <= MAX_SIGMA, ("unstructured", rms, mx)
 
 
 def test_tc_exp3d_workload_slab(cuda_lib, workloads):
