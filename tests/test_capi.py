@@ -65,3 +65,18 @@ def test_tc_operand_kind_switch(lib):
     assert _native.set_tc_operands("f16") == "tf32"
     with pytest.raises(ValueError):
         _native.set_tc_operands("bf16")
+
+
+def test_tc_tile_width_choice(lib):
+    """The tensor-core grid path's z tile (MMA N) for a last axis of nz
+    points: fewest tile-times, then least padding, then the wider tile (host
+    code, no device needed)."""
+    expect = {1: 128, 40: 128, 128: 128, 129: 192, 192: 192, 193: 256, 256: 256,
+              320: 192, 384: 192, 640: 256, 1000: 256, 4096: 256}
+    for nz, nt in expect.items():
+        assert lib.gst_grid_tc_tile_cols(nz) == nt, nz
+    assert lib.gst_grid_tc_tile_cols(-1) == -1
+    # never more padded columns than the 256-wide tile
+    for nz in range(1, 2000, 7):
+        nt = lib.gst_grid_tc_tile_cols(nz)
+        assert -(-nz // nt) * nt <= -(-nz // 256) * 256 or nt == 256, nz
