@@ -172,6 +172,42 @@ def test_gpu_matches_recorded_cases(cuda_lib, ref_goldens):
                                        err_msg=name)
 
 
+def test_fp32_distance_error_bound():
+    """The fast variogram kernel's squared distance, emulated in numpy
+    float32 (hi + lo coordinate splits, the kernel's operation order):
+    within B = 2^-21 d2 + 2^-44 X sqrt(d2) + 2^-90 X^2 of the FP64 value
+    (X the largest |coordinate|), on clouds from 1e-6 to 1e12 with close
+    and far pairs; the kernel's guard is at least 4 B."""
+    f32 = np.float32
+    rng = np.random.default_rng(7)
+    worst = 0.0
+    for trial in range(400):
+        off = 10.0 ** rng.uniform(-6, 12)
+        spread = off * 10.0 ** rng.uniform(-12, 1) + 1e-3 * rng.uniform()
+        dim = int(rng.integers(1, 4))
+        xj = off + spread * rng.uniform(-1, 1, (dim, 500))
+        xk = off + spread * rng.uniform(-1, 1, (dim, 500))
+        if trial % 3 == 0:
+            xk = xj + spread * 1e-6 * rng.uniform(-1, 1, (dim, 500))
+        hj, hk = xj.astype(f32), xk.astype(f32)
+        lj = (xj - hj.astype(np.float64)).astype(f32)
+        lk = (xk - hk.astype(np.float64)).astype(f32)
+        dx = ((hj - hk) + (lj - lk)).astype(f32)
+        f2 = (dx[0] * dx[0]).astype(f32)
+        for d in range(1, dim):   # fmaf: one rounding of the exact sum
+            f2 = (f2.astype(np.float64) + dx[d].astype(np.float64) ** 2).astype(f32)
+        d2 = np.zeros(xj.shape[1])
+        for d in range(dim):
+            d2 = d2 + (xj[d] - xk[d]) ** 2
+        big_x = max(np.abs(hj).max(), np.abs(hk).max())
+        bound = 2.0**-21 * d2 + 2.0**-44 * big_x * np.sqrt(d2) + 2.0**-90 * big_x**2
+        ok = d2 > 0
+        if ok.any():
+            err = np.abs(f2.astype(np.float64) - d2)[ok] / bound[ok]
+            worst = max(worst, float(err.max()))
+    assert 0.0 < worst <= 1.0, worst
+
+
 def test_angle_boundary_double_double():
     """cos of the rounding boundary of the angle tolerance (host code of the
     library, no device): against 200-bit arithmetic, and the decisions it
