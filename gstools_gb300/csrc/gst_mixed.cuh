@@ -1,5 +1,6 @@
 // Mixed-precision phase evaluation shared by the pointwise, batched and
-// adjoint kernels.
+// adjoint kernels (phases taken relative to an origin point, see
+// rotate_to_origin below).
 //
 // The phase in turns t = <q, x> with q = k / (2 pi) is reduced modulo 1
 // without FP64 arithmetic per (mode, point):

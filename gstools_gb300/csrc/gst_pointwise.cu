@@ -5,7 +5,8 @@
 // :682-689).  One kernel template covers
 //
 //   KIND   scalar (summate, summate_fourier) or incompressible (summate_incompr)
-//   PREC   FP64 (parity anchor) or mixed (FP32 + SFU, exact turn reduction)
+//   PREC   FP64 (parity anchor) or mixed (FP32 + SFU, split turn reduction
+//          of phases relative to the first point)
 //   POS    unstructured points (pos is (dim, n)) or structured-grid points
 //          addressed through per-axis coordinate arrays (no meshgrid in HBM)
 //
@@ -64,9 +65,12 @@ struct Tiling<kMixed> {
 //
 // FP64 scalar entry  (8 doubles): k0 k1 k2 k3 z1 z2 f -    f = weight (1)
 // FP64 incompr entry (8 doubles): k0 k1 k2 z1 z2 p0 p1 p2   p = projector
-// mixed entry (16 floats): qh0 qh1 qh2 z1 | ql0 ql1 ql2 z2 | p0 p1 p2 - | ...
+// mixed entry (16 floats): qh0 qh1 qh2 a1 | ql0 ql1 ql2 a2 | p0 p1 p2 - | ...
 //                          q = k / (2 pi) split as qh (12 significant bits)
-//                          + ql, so qh * xh is exact in FP32.
+//                          + ql, so qh * xh is exact in FP32; (a1, a2) =
+//                          (z1, z2) rotated by <k, x0>, x0 the first point,
+//                          whose coordinates the kernel subtracts from every
+//                          point (gst_mixed.cuh, rotate_to_origin).
 // `weight` is summate_fourier's spectrum factor: the FP64 table keeps it as a
 // separate factor (applied to z1 cos + z2 sin, as the reference does); the
 // mixed table folds it into z1 and z2.
