@@ -19,6 +19,12 @@
  *              the first matching direction
  *   structured / ma_structured: lags k >= 1 along axis 0 of f (n0, rest),
  *              skipping masked values
+ *
+ * The angle test stays "acos(|s| / dist) < angles_tol" with the host libm's
+ * acos, as in the reference; pairs on the tolerance cone (lattice points at
+ * exactly the tolerance angle) then depend on libm's last bit.  The GPU
+ * kernels decide the same test as a correctly rounded acos would, so the
+ * two agree wherever libm's acos is correctly rounded.
  */
 #include <math.h>
 #include <stdint.h>
