@@ -205,6 +205,28 @@ def test_summators_refuse_without_gpu():
         pytest.skip("a CUDA device is present")
     with pytest.raises(RuntimeError):
         gg.summate(np.ones((2, 3)), np.ones(3), np.ones(3), np.ones((2, 4)))
+    # every public compute entry point fails loudly: there is no CPU fallback
+    import gstools_gb300.variogram as gv
+
+    k, z, x = np.ones((2, 3)), np.ones(3), np.ones((2, 4))
+    axes = [np.arange(4.0), np.arange(5.0)]
+    calls = [
+        lambda: gg.summate(k, z, z, x, precision="mixed"),
+        lambda: gg.summate_incompr(k, z, z, x),
+        lambda: gg.summate_fourier(z, k, z, z, x),
+        lambda: gg.summate_grid(k, z, z, axes, precision="mixed"),
+        lambda: gg.summate_incompr_grid(k, z, z, axes, precision="mixed"),
+        lambda: gg.summate_fourier_grid(z, k, z, z, axes),
+        lambda: gg.calc_field_krige(np.eye(2), np.ones((2, 3)), np.ones(2)),
+        lambda: gg.calc_field_krige_and_variance(np.eye(2), np.ones((2, 3)), np.ones(2)),
+        lambda: gv.unstructured(np.ones((1, 4)), np.arange(3.0), x),
+        lambda: gv.directional(np.ones((1, 4)), np.arange(3.0), x, np.eye(2), 0.3),
+        lambda: gv.structured(np.ones((4, 3))),
+        lambda: gg.BatchedSummator(2, [3], [4]),
+    ]
+    for i, call in enumerate(calls):
+        with pytest.raises(RuntimeError):
+            call()
 
 
 def test_torch_isometrize_matches_numpy():
