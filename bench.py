@@ -7,22 +7,37 @@ sampling, stored in tests/golden/workloads.npz) -- summed on the structured
 evaluations per step.
 
 Metric: G mode*point evals/s of the fastest path at its stated error against
-the FP64 kernel, with the plain FP64 kernel's throughput reported beside it.
+the FP64 oracle, with the plain FP64 kernel's throughput reported beside it.
 
 * ``value``  -- device-resident inputs, CUDA-event timing of one step of the
                 separable tensor-core path (per-axis tables + 3xFP16
                 contraction, FP32 accumulation; L2 flushed between steps);
+* ``error_vs_fp64`` -- the headline output against the FP64 C oracle: on a
+                32^3 sub-grid recomputed here, and on the sub-grid the
+                reference's own pipeline (its RNG, its isometrized meshgrid)
+                evaluated when the fixture was made;
 * ``e2e``    -- the public API ``gstools_gb300.summate_grid`` called with host
                 numpy arrays: host->device copy of the modes and axes, the
                 kernels, and the device->host copy of the float32 field, all
-                inside the timed region;
-* ``f64_plain`` / ``other_paths`` -- the plain FP64 kernel (on a slab) and
-                the mixed-precision pointwise kernel on the same workload;
+                inside the timed region (clocks sampled over it);
+* ``e2e_reference_call`` -- the summation a structured ``SRF`` of the
+                reference runs once ``install()`` routes it
+                (``summate_structured``: unmapped modes, isometrize matrix,
+                axes in; the float64 flat field the reference expects out);
+* ``f64_plain`` / ``other_paths`` -- the plain FP64 kernel (on a slab), the
+                mixed-precision pointwise kernel on the same workload, and
+                bounded runs of the other four configurations (2-D points,
+                512-realization ensemble, incompressible 192^3 field,
+                gradients), each with its error against the oracle and its
+                own clock record;
 * ``cpu_baseline`` -- the FP64 C/OpenMP oracle on a bounded slab of the same
                 grid, all host cores;
 * ``--impl reference`` -- the same oracle as the reference arm (the
                 reference's own kernels are in the external gstools-cython
-                package and cannot be built here), on the same config.
+                package and cannot be built here), on the same config: each
+                step is a bounded slab of the grid; the line reports the
+                throughput, the measured time of a step and the points it
+                covered.
 
 Defaults: 200 timed steps after 3 warm-up steps (about 70 ms of timed
 work, so the 10 ms clock sampler sees the timed region); ``clocks`` reports
@@ -54,8 +69,9 @@ GRID = 256
 N_MODES = 2000
 VAR = 2.0
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
-# DRAM bytes (read + write) of one contraction launch on this workload, from
-# the ncu capture summarised in profiles/grid_tc_kernel_exp3d_grid256.md.
+# DRAM bytes (read + write) of one contraction launch on this workload
+# (dram__bytes_read.sum + dram__bytes_write.sum of grid_tc_kernel, one ncu
+# capture of this build).
 TC_DRAM_BYTES_PER_LAUNCH = 34.6e6
 
 
@@ -71,6 +87,9 @@ def parse():
     p.add_argument("--path", default="auto",
                    choices=["auto", "mixed", "tensor", "f64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-workloads", dest="workloads", action="store_false",
+                   help="leave the bounded runs of the other configurations "
+                        "out of the headline line")
     p.add_argument("--size", default="full", choices=["full", "small"],
                    help="small: reduced problem sizes of the krige and vario "
                         "workloads (for profiler captures)")
@@ -178,6 +197,22 @@ class Clocks:
                 "interval_ms": 10}
 
 
+def workload_config(n, world):
+    """The ``config`` of both arms' lines (identical keys and values)."""
+    return {"workload": f"exp3d_grid{n}_modes{N_MODES}",
+            "model": "Exponential(dim=3, var=2, len_scale=[20,10,5])",
+            "grid": [n, n, n], "modes": N_MODES,
+            "mode_points_per_step": N_MODES * n ** 3,
+            "parallelism": f"replicas x{world}"}
+
+
+def _grid_sample(axes, n):
+    """The first n points of the grid spanned by axes (flattened "ij")."""
+    shape = tuple(len(a) for a in axes)
+    idx = np.unravel_index(np.arange(n), shape)
+    return np.array([a[i] for a, i in zip(axes, idx)])
+
+
 def cpu_baseline(cov, z1, z2, axes, target_s=10.0):
     """FP64 C/OpenMP oracle on the first points of the grid (flattened "ij"
     order), sized for about ``target_s`` seconds on all host cores."""
@@ -187,23 +222,19 @@ def cpu_baseline(cov, z1, z2, axes, target_s=10.0):
     threads = oracle.num_threads()
     shape = tuple(len(a) for a in axes)
     total = int(np.prod(shape))
-
-    def sample(n):
-        idx = np.unravel_index(np.arange(n), shape)
-        return np.array([a[i] for a, i in zip(axes, idx)])
-
-    pts = sample(min(total, 65536))
+    pts = _grid_sample(axes, min(total, 65536))
     t0 = time.perf_counter()
     oracle.c_summate(cov, z1, z2, pts)
     dt = time.perf_counter() - t0
     rate = cov.shape[1] * pts.shape[1] / max(dt, 1e-6)
     n = int(np.clip(rate * target_s / cov.shape[1], 1, total))
-    pts = sample(n)
+    pts = _grid_sample(axes, n)
     t0 = time.perf_counter()
     oracle.c_summate(cov, z1, z2, pts)
     dt = time.perf_counter() - t0
     value = cov.shape[1] * n / dt / 1e9
     return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "points_timed": n, "seconds": dt,
             "sample": (f"FP64 C/OpenMP oracle, {cov.shape[1]} modes x {n} "
                        f"grid points (the first {n} of the "
                        f"{'x'.join(map(str, shape))} grid), {dt:.2f} s on "
@@ -211,6 +242,11 @@ def cpu_baseline(cov, z1, z2, axes, target_s=10.0):
 
 
 def run_reference(args):
+    """The reference arm: the FP64 C/OpenMP restatement of the reference's
+    summate on the same workload, all host cores.  A step is a bounded slab
+    of the grid (the same first points every step), sized so the whole run
+    takes about two and a half minutes; ``value`` is its throughput and
+    ``ms_per_step`` its measured time."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -219,30 +255,38 @@ def run_reference(args):
     import oracle
 
     oracle.build()
-    vals = []
-    base = None
-    # each step a bounded sample: the whole run stays near two and a half
-    # minutes whatever --steps is
+    threads = oracle.num_threads()
     per_step_s = float(np.clip(150.0 / (args.warmup + args.steps), 0.2, 5.0))
+    # size the slab once, then time every step on the same points
+    probe = cpu_baseline(cov, z1, z2, axes, target_s=per_step_s)
+    n = probe["points_timed"]
+    pts = _grid_sample(axes, n)
+    times = []
     for i in range(args.warmup + args.steps):
-        base = cpu_baseline(cov, z1, z2, axes, target_s=per_step_s)
+        t0 = time.perf_counter()
+        oracle.c_summate(cov, z1, z2, pts)
+        dt = time.perf_counter() - t0
         if i >= args.warmup:
-            vals.append(base["value"])
-    value = statistics.median(vals)
-    base["value"] = value
-    full_step_ms = N_MODES * args.grid ** 3 / (value * 1e9) * 1e3
+            times.append(dt)
+    t_step = statistics.mean(times)
+    value = N_MODES * n / t_step / 1e9
+    sample = (f"FP64 C/OpenMP oracle, {N_MODES} modes x {n} grid points (the "
+              f"first {n} of the {args.grid}^3 grid) per step, {threads} "
+              f"threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": full_step_ms,
-        "ms_per_step_note": "extrapolated from the timed sample to the full grid",
+        "ms_per_step": t_step * 1e3,
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"exp3d_grid{args.grid}_modes{N_MODES}",
-                   "grid": [args.grid] * 3, "modes": N_MODES,
-                   "model": "Exponential(dim=3, var=2, len_scale=[20,10,5])",
-                   "l2": "inputs smaller than L2; CPU run"},
-        "cpu_baseline": base,
+        "config": workload_config(args.grid, world),
+        "points_timed": n,
+        "full_grid_ms_extrapolated": N_MODES * args.grid ** 3 / (value * 1e9) * 1e3,
+        "notes": {"step": "a bounded slab of the grid; value = its mode*point "
+                          "throughput (linear in points)",
+                  "l2": "CPU run", "output": "float64"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
+                         "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": ("reference summators (gstools-cython / gstools_core) are "
@@ -421,17 +465,38 @@ def run_ours(args):
     value = world * work / t_step / 1e9
     t_main = max_over_ranks(statistics.mean(per_part[-1]))
 
-    # -- error of the headline output vs the FP64 kernel on a sub-grid ------
+    # -- error of the headline output vs the FP64 oracle --------------------
+    import oracle
+
+    oracle.build()
     stride = max(1, n // 32)
     sub = [a[::stride] for a in axes]
-    ref64 = gg.summate_grid(cov, z1, z2, sub, scale=scale)
-    got = out32[::stride, ::stride, ::stride].double().cpu().numpy()
+    pts_sub = np.array(np.meshgrid(*sub, indexing="ij")).reshape(3, -1)
+    ref64 = scale * oracle.c_summate(cov, z1, z2, pts_sub)
+    got = out32[::stride, ::stride, ::stride].double().cpu().numpy().reshape(-1)
     diff = got - ref64
     sigma = np.sqrt(VAR)
     err = {"rms_sigma": float(np.sqrt(np.mean(diff**2)) / sigma),
            "max_abs_sigma": float(np.max(np.abs(diff)) / sigma),
-           "vs": "FP64 grid kernel (reference op order)",
+           "vs": "FP64 C oracle (reference formula and operation order), "
+                 "mapped modes on the raw sub-grid",
            "points": int(diff.size)}
+    if n == GRID:
+        # the sub-grid the reference's own pipeline evaluated (its RNG, its
+        # isometrized meshgrid, the oracle as its summator) for the fixture
+        wl = np.load(os.path.join(ROOT, "tests", "golden", "workloads.npz"))
+        ix = [torch.from_numpy(wl[f"exp3d/sub_{c}"].astype(np.int64)).to(dev)
+              for c in "xyz"]
+        got_ref = out32.index_select(0, ix[0]).index_select(1, ix[1]) \
+            .index_select(2, ix[2])
+        d_ref = got_ref.double().cpu().numpy().reshape(-1) - \
+            scale * wl["exp3d/summed_sub"]
+        err["reference_pipeline"] = {
+            "rms_sigma": float(np.sqrt(np.mean(d_ref**2)) / sigma),
+            "max_abs_sigma": float(np.max(np.abs(d_ref)) / sigma),
+            "points": int(d_ref.size),
+            "vs": "the reference's RandMeth on its isometrized meshgrid with "
+                  "the FP64 oracle as summator (fixture)"}
 
     # -- the other paths, for the record ------------------------------------
     others = {}
@@ -509,20 +574,52 @@ def run_ours(args):
                                method=method, out_dtype="float32",
                                scale=scale)
 
-    for _ in range(2):
-        res = step_e2e()
-    torch.cuda.synchronize()
-    barrier()
-    e2e_times = []
-    for _ in range(max(3, min(args.steps, 5))):
-        flush.fill_(1.0)
+    def host_timed(fn, calls, warmup=3):
+        """Wall-clock time per call of fn (host inputs and result), L2
+        flushed before each call, clocks sampled over the loop."""
+        for _ in range(warmup):
+            res = fn()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        res = step_e2e()
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_t = max_over_ranks(statistics.mean(e2e_times))
+        barrier()
+        ck = Clocks(local)
+        ck.start()
+        times = []
+        t_begin = time.time()
+        for _ in range(calls):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = fn()
+            times.append(time.perf_counter() - t0)
+        window_e2e = (t_begin, time.time())
+        return res, max_over_ranks(statistics.mean(times)), ck.stop(window_e2e)
+
+    e2e_calls = max(20, min(args.steps, 200))
+    res, e2e_t, e2e_clk = host_timed(step_e2e, e2e_calls)
     h2d = cov.nbytes + z1.nbytes + z2.nbytes + sum(a.nbytes for a in axes)
     d2h = res.nbytes
+
+    # -- the routed structured SRF call of the reference ---------------------
+    # install() hands a structured SRF evaluation to summate_structured with
+    # the generator's (unmapped) modes, the model's isometrize matrix and the
+    # axis arrays, and returns the float64 flat sum the reference scales.
+    wl = np.load(os.path.join(ROOT, "tests", "golden", "workloads.npz"))
+    cov_raw, iso = wl["exp3d/cov"], wl["exp3d/isometrize"]
+
+    def step_routed():
+        return gg.summate_structured(cov_raw, z1, z2, axes, iso,
+                                     precision="mixed")
+
+    res_r, routed_t, routed_clk = host_timed(step_routed, max(20, e2e_calls // 4))
+    routed = {"value": world * work / routed_t / 1e9, "unit": UNIT,
+              "ms_per_call": routed_t * 1e3, "calls": max(20, e2e_calls // 4),
+              "h2d_bytes_per_step": int(cov_raw.nbytes + z1.nbytes + z2.nbytes
+                                        + iso.nbytes
+                                        + sum(a.nbytes for a in axes)),
+              "d2h_bytes_per_step": int(res_r.nbytes),
+              "output": "float64 (the reference's summator contract)",
+              "clocks": routed_clk}
+    del res_r
 
     # -- roofline of the dominant kernel -------------------------------------
     peaks = {"fp32_tflops": peak_probe(torch, 0, 4096) / 1e12,
@@ -576,16 +673,9 @@ def run_ours(args):
         "dtype": (f"{args.operands}x3 (fp32 accumulate)" if path == "tensor"
                   else "fp32 + exact turn reduction"),
         "data": "synthetic (modes from the reference RNG, fixture)",
-        "config": {
-            "workload": f"exp3d_grid{n}_modes{N_MODES}",
-            "model": "Exponential(dim=3, var=2, len_scale=[20,10,5])",
-            "grid": [n, n, n], "modes": N_MODES,
-            "mode_points_per_step": work,
-            "path": desc,
-            "output": "float32, scaled by sqrt(var/N)",
-            "l2": "512 MB buffer written between timed steps",
-            "parallelism": f"replicas x{world}",
-        },
+        "config": workload_config(n, world),
+        "notes": {"path": desc, "output": "float32, scaled by sqrt(var/N)",
+                  "l2": "512 MB buffer written between timed steps"},
         "error_vs_fp64": err,
         "f64_plain": {"value": f64_value, "unit": UNIT,
                       "sample": f"{slab}x{n}x{n} slab, FP64 grid kernel",
@@ -593,7 +683,10 @@ def run_ours(args):
         "other_paths": others,
         "e2e": {"value": world * work / e2e_t / 1e9, "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h),
+                "calls": e2e_calls, "ms_per_call": e2e_t * 1e3,
+                "clocks": e2e_clk},
+        "e2e_reference_call": routed,
         "roofline": roof,
         "measured_peaks": peaks,
         "clocks": clk,
@@ -601,6 +694,8 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cov, z1, z2, axes)
+    if args.workloads and world == 1 and n == GRID:
+        line["other_paths"]["configs"] = other_configs(args, torch, gg, flush)
     if world > 1:
         import torch.distributed as dist
 
@@ -858,10 +953,12 @@ def wl_points(args, torch, gg, flush):
     got64 = f64().cpu().numpy()
     gotmx = mixed().cpu().numpy()
     s = np.sqrt(1.0 / 1000)
+    e2e = gg.summate(gen.cov_samples, gen.z_1, gen.z_2, pos, precision="mixed")
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(3):
+    for _ in range(20):
         e2e = gg.summate(gen.cov_samples, gen.z_1, gen.z_2, pos, precision="mixed")
-    te2e = (time.perf_counter() - t0) / 3
+    te2e = (time.perf_counter() - t0) / 20
     return _line(
         args, "gau2d_points100k_modes1000", work / tmx / 1e9, tmx,
         "fp32 + exact turn reduction", {"points": 100_000, "modes": 1000},
@@ -869,7 +966,8 @@ def wl_points(args, torch, gg, flush):
                    "max_rel_err_vs_oracle": float(np.max(np.abs(got64 - ref))
                                                   / np.max(np.abs(ref)))},
         error_vs_fp64={"rms_sigma": float(np.sqrt(np.mean((s * (gotmx - ref)) ** 2))),
-                       "max_abs_sigma": float(np.max(np.abs(s * (gotmx - ref))))},
+                       "max_abs_sigma": float(np.max(np.abs(s * (gotmx - ref)))),
+                       "vs": "FP64 C oracle, all 100 000 points"},
         e2e={"value": work / te2e / 1e9, "unit": UNIT,
              "h2d_bytes_per_step": int(pos.nbytes + 4 * 8 * 1000),
              "d2h_bytes_per_step": int(e2e.nbytes)},
@@ -965,9 +1063,22 @@ def wl_ensemble(args, torch, gg, flush):
     t_seqmx = _timed_events(
         torch, lambda: sequential("gst_summate_mixed", [_native.GST_OUT_F64]),
         2, 1, flush)
-    err = np.sqrt(sum(float(np.sum((b - r) ** 2)) for b, r in zip(batched, ref))
-                  / sum(len(r) for r in ref))
-    mx = max(float(np.max(np.abs(b - r))) for b, r in zip(batched, ref))
+    import oracle
+
+    # every realization against the FP64 oracle on 256 of its points
+    rng_s = np.random.RandomState(3)
+    sq, cnt, mx, worst = 0.0, 0, 0.0, 0.0
+    for r, g in enumerate(gens):
+        idx = np.sort(rng_s.choice(pts[r], size=min(256, pts[r]), replace=False))
+        ref_o = scales[r] * oracle.c_summate(g.cov_samples, g.z_1, g.z_2,
+                                             np.ascontiguousarray(pos[r][:, idx]))
+        d = batched[r][idx] - ref_o
+        sq += float(np.sum(d ** 2))
+        cnt += d.size
+        mx = max(mx, float(np.max(np.abs(d))))
+        worst = max(worst, float(np.sqrt(np.mean(d ** 2))))
+    err = np.sqrt(sq / cnt)
+    seq_err = max(float(np.max(np.abs(b - r))) for b, r in zip(batched, ref))
     # end to end: host arrays in, per-realization host arrays out
     cov_l = [g.cov_samples for g in gens]
     z1_l = [g.z_1 for g in gens]
@@ -977,8 +1088,6 @@ def wl_ensemble(args, torch, gg, flush):
     t0 = time.perf_counter()
     res = bs(cov_l, z1_l, z2_l, pos, scales)
     te2e = time.perf_counter() - t0
-    import oracle
-
     cpu = _cpu_sample(
         lambda r: oracle.c_summate(gens[r].cov_samples, gens[r].z_1, gens[r].z_2, pos[r]),
         list(range(len(gens))), lambda r: modes[r] * pts[r], what="realizations",
@@ -1001,7 +1110,10 @@ def wl_ensemble(args, torch, gg, flush):
                                    "(not the reference's MT19937 stream)"},
         sample_and_sum={"value": work / t_ss / 1e9, "unit": UNIT,
                         "ms": t_ss * 1e3},
-        error_vs_fp64={"rms_sigma": err, "max_abs_sigma": mx},
+        error_vs_fp64={"rms_sigma": err, "max_abs_sigma": mx,
+                       "worst_realization_rms_sigma": worst,
+                       "vs": "FP64 C oracle, 256 points of every realization",
+                       "max_abs_vs_sequential_fp64_gpu": seq_err},
         e2e={"value": work / te2e / 1e9, "unit": UNIT,
              "h2d_bytes_per_step": int(sum(p.nbytes for p in pos)
                                        + sum(c.nbytes for c in cov_l) * 2),
@@ -1046,10 +1158,26 @@ def wl_incompr(args, torch, gg, flush):
     t64 = _timed_events(torch, f64, 1, 1, flush)
     mixed()
     tensor()
-    got = out[:, :slab].double().cpu().numpy()
-    ref = scale * out64.cpu().numpy()
-    diff = got - ref
-    diff_tc = out_tc[:, :slab].double().cpu().numpy() - ref
+    import oracle
+
+    # the FP64 oracle on every 8th grid point per axis (24^3 points)
+    sub = np.arange(0, n, 8)
+    pts_sub = np.array(np.meshgrid(sub, sub, sub, indexing="ij"),
+                       dtype=np.float64).reshape(3, -1)
+    ref = scale * oracle.c_summate_incompr(cov, z1, z2, pts_sub)
+    isub = torch.from_numpy(sub).to(dev)
+
+    def at_sub(t):
+        t = t.index_select(1, isub).index_select(2, isub).index_select(3, isub)
+        return t.double().cpu().numpy().reshape(3, -1)
+
+    diff = at_sub(out) - ref
+    diff_tc = at_sub(out_tc) - ref
+    # the FP64 kernel's slab (x < 12) at the sub-grid points it covers
+    ref4 = ref.reshape(3, len(sub), len(sub), len(sub))
+    xs = np.nonzero(sub < slab)[0]
+    o64 = scale * out64.cpu().numpy()[:, sub[xs]][:, :, ::8, ::8]
+    f64_rel = float(np.max(np.abs(o64 - ref4[:, xs])) / np.max(np.abs(ref4[:, xs])))
     # divergence of the float32 field by central differences (unit spacing)
     u = out_tc.double()
     div = ((u[0, 2:, 1:-1, 1:-1] - u[0, :-2, 1:-1, 1:-1])
@@ -1074,11 +1202,14 @@ def wl_incompr(args, torch, gg, flush):
         {"grid": [n] * 3, "modes": nm, "components": 3, "output": "float32",
          "path": "tensor-core grid path, one weighted contraction per component"},
         f64_plain={"value": nm * slab * n * n / t64 / 1e9, "unit": UNIT,
-                   "sample": f"{slab}x{n}x{n} slab"},
+                   "sample": f"{slab}x{n}x{n} slab",
+                   "max_rel_err_vs_oracle": f64_rel},
         mixed_pointwise={"value": work / tmx / 1e9, "unit": UNIT,
                          "rms_sigma": float(np.sqrt(np.mean(diff ** 2)))},
         error_vs_fp64={"rms_sigma": float(np.sqrt(np.mean(diff_tc ** 2))),
-                       "max_abs_sigma": float(np.max(np.abs(diff_tc)))},
+                       "max_abs_sigma": float(np.max(np.abs(diff_tc))),
+                       "vs": "FP64 C oracle on every 8th grid point per axis "
+                             f"({pts_sub.shape[1]} points, 3 components)"},
         divergence={"fd_rms_over_grad_rms": float(div.std() / grad_scale),
                     "note": "central differences, h=1; O(h^2) truncation"},
         cpu_baseline=cpu,
@@ -1090,7 +1221,7 @@ def wl_adjoint(args, torch, gg, flush):
     128^3 grid + 50 000 points in [0, 128]^3; loss = mean squared misfit at
     10 000 random observation points against a field from another seed;
     gradients w.r.t. z_1, z_2, len_scale, anisotropy and rotation angles."""
-    from gstools_gb300.grad import randmeth_field
+    from gstools_gb300.grad import isometrize_matrix, randmeth_field
 
     data = np.load(os.path.join(ROOT, "tests", "golden", "workloads.npz"))
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -1143,6 +1274,18 @@ def wl_adjoint(args, torch, gg, flush):
     work = 4000 * pts.shape[1]
     import oracle
 
+    # forward field vs the FP64 oracle on 4096 of the points
+    with torch.no_grad():
+        u_mx = fwd("mixed").cpu().numpy()
+        k_map = (isometrize_matrix(3, params["angles"], params["anis"]).T
+                 @ cov_ref).cpu().numpy()
+    sel = np.sort(np.random.RandomState(11).choice(pts.shape[1], 4096,
+                                                   replace=False))
+    u_or = np.sqrt(1.0 / 4000) * oracle.c_summate(
+        k_map, data["gau3d_grad/z1"], data["gau3d_grad/z2"],
+        np.ascontiguousarray(pts[:, sel]))
+    d_fwd = u_mx[sel] - u_or
+
     cov_np = data["gau3d_grad/cov"]
     z1_np, z2_np = data["gau3d_grad/z1"], data["gau3d_grad/z2"]
     chunks = list(range(0, pts.shape[1], 4096))
@@ -1156,7 +1299,33 @@ def wl_adjoint(args, torch, gg, flush):
         "fp32 + exact turn reduction",
         {"points": int(pts.shape[1]), "modes": 4000, "observations": 10_000},
         fwd_ms=t_f * 1e3, fwd_bwd_ms=t_fb * 1e3, fwd_bwd_over_fwd=t_fb / t_f,
+        error_vs_fp64={"rms_sigma": float(np.sqrt(np.mean(d_fwd ** 2))),
+                       "max_abs_sigma": float(np.max(np.abs(d_fwd))),
+                       "vs": "FP64 C oracle, forward field at 4096 points"},
         grad_rel_err_mixed_vs_f64=rel, cpu_baseline=cpu, gpu_launches=None)
+
+
+_LINE_ONLY = ("metric", "n_gpus", "steps", "warmup", "higher_is_better",
+              "scaling", "vs_baseline", "data")
+
+
+def other_configs(args, torch, gg, flush):
+    """Bounded runs of the other four configurations for the headline line:
+    5 timed steps after 3 warm-up steps each, every one with its error
+    against the oracle and the clocks sampled over its own run."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup, sub.size = 5, 3, "full"
+    out = {}
+    for fn in (wl_points, wl_ensemble, wl_incompr, wl_adjoint):
+        ck = Clocks(torch.cuda.current_device())
+        ck.start()
+        line = fn(sub, torch, gg, flush)
+        clk = ck.stop()
+        keep = {k: v for k, v in line.items() if k not in _LINE_ONLY}
+        keep["clocks"] = clk
+        keep["steps"], keep["warmup"] = sub.steps, sub.warmup
+        out[line["config"]["workload"]] = keep
+    return out
 
 
 def run_workload(args):

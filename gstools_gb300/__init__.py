@@ -7,7 +7,9 @@ and ``IncomprRandMeth`` (src/gstools/field/generator.py:22-24, 42-64):
   reference's signatures ``(cov_samples, z_1, z_2, pos, num_threads=None)``;
 * :func:`install` -- rebinds ``gstools.field.generator._summate`` /
   ``_summate_incompr`` / ``_summate_fourier`` so an unmodified
-  ``gstools.SRF(model, generator="RandMeth", mode_no=...)`` runs on the GPU;
+  ``gstools.SRF(model, generator="RandMeth", mode_no=...)`` runs on the GPU,
+  and sends structured SRF / CondSRF evaluations to the separable grid
+  kernels (:func:`summate_structured`) without building the meshgrid;
 * :class:`RandMeth`, :class:`IncomprRandMeth`, :class:`SRF` and the models
   :class:`Gaussian`, :class:`Exponential`, :class:`Matern` -- a standalone
   mirror of the reference's generator stack with the same seeds and streams.
@@ -31,6 +33,7 @@ from .summator import (
     summate_grid,
     summate_incompr,
     summate_incompr_grid,
+    summate_structured,
 )
 
 __version__ = "0.1.0"
@@ -56,6 +59,7 @@ __all__ = [
     "summate_grid",
     "summate_incompr_grid",
     "summate_fourier_grid",
+    "summate_structured",
     "install",
     "uninstall",
 ]

@@ -237,7 +237,16 @@ __global__ void __launch_bounds__(kThreads, 2) batched_kernel(const BatchArgs a)
             }
 #pragma unroll
             for (int p = 0; p < P; ++p) acc[p] += static_cast<double>(accf[p]);
-            if (__syncthreads_or(!got)) { ok = false; break; }
+            if (__syncthreads_or(!got)) {
+                // mode tiles mt, mt + 1 may still be landing in shared
+                // memory: drain them before the CTA exits
+                if (tid == 0)
+                    mbar_drain(full_bar, 2, gidx,
+                               consumed + static_cast<uint64_t>(min(mt + 2, n_mt)),
+                               a.err);
+                ok = false;
+                break;
+            }
             if (tid == 0 && mt + 2 < n_mt) {
                 mbar_arrive_expect_tx(&full_bar[slot], kStageBytes);
                 bulk_copy_g2s(stage[slot], src + (mt + 2) * kStageBytes,

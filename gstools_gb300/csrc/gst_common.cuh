@@ -158,6 +158,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
     }
 }
 
+// After a failed wait: waits (each bounded like mbar_wait) for every bulk
+// copy still in flight into this CTA's ring of `n_stages` barriers -- the
+// global stage indices [first, last), stage u on barrier u % n_stages with
+// parity (u / n_stages) & 1 -- so that the CTA does not exit while the copy
+// engine still writes into its shared memory.  One thread calls it.
+__device__ __forceinline__ void mbar_drain(uint64_t *bars, int n_stages,
+                                           uint64_t first, uint64_t last,
+                                           unsigned int *err) {
+    for (uint64_t u = first; u < last; ++u)
+        mbar_wait(&bars[u % n_stages],
+                  static_cast<uint32_t>((u / n_stages) & 1u), err);
+}
+
 // Bulk (TMA) copy global -> shared, completion signalled on `bar` as
 // transaction bytes.  Both addresses 16-byte aligned, bytes % 16 == 0.
 __device__ __forceinline__ void bulk_copy_g2s(void *smem_dst,

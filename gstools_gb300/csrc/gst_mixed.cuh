@@ -57,6 +57,27 @@ __device__ __forceinline__ float mixed_turns(const float (&qh)[3],
     return __fsub_rn(r, __fsub_rn(__fadd_rn(r, kRoundMagicF), kRoundMagicF));
 }
 
+// Reduced turns of <q, x> - psi (psi in [-1/2, 1/2]), in [-1/2, 1/2]: the
+// split reduction above with psi folded into the cross terms.
+template <int DIM>
+__device__ __forceinline__ float mixed_turns_minus(const float (&qh)[3],
+                                                   const float (&ql)[3],
+                                                   const MixedPoint<DIM> &p,
+                                                   float psi) {
+    float r = 0.0f, cross = -psi;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const float prod = __fmul_rn(qh[d], p.xh[d]);
+        const float nint = __fsub_rn(__fadd_rn(prod, kRoundMagicF), kRoundMagicF);
+        const float frac = __fsub_rn(prod, nint);
+        r = (d == 0) ? frac : __fadd_rn(r, frac);
+        cross = fmaf(qh[d], p.xl[d], cross);
+        cross = fmaf(ql[d], p.xf[d], cross);
+    }
+    r = __fadd_rn(r, cross);
+    return __fsub_rn(r, __fsub_rn(__fadd_rn(r, kRoundMagicF), kRoundMagicF));
+}
+
 template <int DIM>
 __device__ __forceinline__ void mixed_sincos(const float (&qh)[3],
                                              const float (&ql)[3],

@@ -313,7 +313,14 @@ __global__ void __launch_bounds__(Tiling<PREC>::kThreads,
         }
 
         // Stage s fully consumed by every thread; agree on wait failures.
-        if (__syncthreads_or(!ok)) break;
+        // On a failure, tiles t .. t + kStages - 1 may still be landing in
+        // shared memory: drain them before the CTA exits.
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0)
+                mbar_drain(full_bar, kStages, static_cast<uint64_t>(t),
+                           static_cast<uint64_t>(min(t + kStages, n_tile)), a.err);
+            break;
+        }
         if (tid == 0 && t + kStages < n_tile) {
             mbar_arrive_expect_tx(&full_bar[s], kStageBytes);
             bulk_copy_g2s(stage[s], a.table + (tile0 + t + kStages) * kStageBytes,
@@ -763,7 +770,8 @@ int gst_summate_incompr_grid_mixed(int dim, int64_t n_modes,
 // * Host code cannot use the array's name as a device address.  The first
 //   call on each device (with that device current) looks the address up
 //   with cudaGetSymbolAddress and caches it; make that first call before
-//   any stream capture.
+//   any stream capture (a first call on a capturing stream is refused with
+//   GST_ERR_INVALID_ARGUMENT).
 // * Every call shares the one array, which keeps the previous call's
 //   contents.  Nothing in it has to start at zero (each call overwrites the
 //   table and every partial sum it reads), but calls that overlap on the
@@ -799,10 +807,23 @@ int noalloc_scratch(unsigned char **ptr) {
             note_cuda_error(e);
             return GST_ERR_CUDA;
         }
+        // the other per-device lookups of this entry point, done here so
+        // that a call under capture never performs them
+        if (device_error_word() == nullptr) return GST_ERR_CUDA;
+        (void)sm_count();
         g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
     }
     *ptr = g_noalloc_ptr[dev];
     return GST_OK;
+}
+
+// Whether the first-call set-up (scratch address, error word, SM count) of
+// the current device is done.
+bool noalloc_ready() {
+    const int dev = current_device();
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return false;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    return g_noalloc_ptr[dev] != nullptr;
 }
 
 int run_noalloc_f64(const Request &r) {
@@ -817,6 +838,14 @@ int run_noalloc_f64(const Request &r) {
         return GST_OK;
     }
     if (r.cov == nullptr || r.z1 == nullptr || r.z2 == nullptr || r.pos == nullptr)
+        return GST_ERR_INVALID_ARGUMENT;
+
+    // The first call on a device looks up addresses (cudaGetSymbolAddress)
+    // and the SM count; inside a stream capture that set-up is refused with
+    // a clear status instead of failing in the middle of the capture.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    GST_TRY_CUDA(cudaStreamIsCapturing(r.stream, &capture));
+    if (capture != cudaStreamCaptureStatusNone && !noalloc_ready())
         return GST_ERR_INVALID_ARGUMENT;
 
     unsigned char *scratch = nullptr;

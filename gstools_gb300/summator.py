@@ -34,6 +34,8 @@ __all__ = [
     "summate_grid",
     "summate_incompr_grid",
     "summate_fourier_grid",
+    "summate_structured",
+    "structured_supported",
     "device",
 ]
 
@@ -461,3 +463,95 @@ def summate_fourier_grid(spectrum_factor, modes, z_1, z_2, axes, *,
                  _p(fac), _p(kk), _p(z1), _p(z2), _p(out), code, float(scale),
                  _stream(dev))
     return _finish(out, as_torch)
+
+
+_KINDS = ("scalar", "incompr", "fourier")
+
+
+def _iso_matrix(iso, dim):
+    if iso is None:
+        return np.eye(dim)
+    m = np.asarray(iso, dtype=np.float64)
+    if m.shape != (dim, dim):
+        raise ValueError(f"iso must be a ({dim}, {dim}) matrix")
+    return m
+
+
+def structured_supported(kind, dim, precision=None, iso=None):
+    """Whether :func:`summate_structured` evaluates this case on the grid
+    kernels: scalar sums in any precision (dim 1-3); incompressible sums in
+    mixed precision (dim 2-3, tensor cores) or in FP64 when the isometrize
+    map is the identity (the FP64 grid kernel takes the projector from the
+    phase wave vectors); Fourier sums in mixed precision (dim 2-3)."""
+    prec = config.check_precision(precision)
+    if kind not in _KINDS:
+        raise ValueError(f"kind must be one of {_KINDS}")
+    if not 1 <= dim <= 3:
+        return False
+    if kind == "scalar":
+        return True
+    if dim not in (2, 3):
+        return False
+    if kind == "incompr":
+        return prec == "mixed" or iso is None or np.array_equal(
+            np.asarray(iso, dtype=np.float64), np.eye(dim))
+    return prec == "mixed"
+
+
+def summate_structured(cov_samples, z_1, z_2, axes, iso=None, *,
+                       kind="scalar", spectrum_factor=None, precision=None):
+    """The reference summators on a structured grid, with their flat result.
+
+    Returns what ``summate`` / ``summate_incompr`` / ``summate_fourier``
+    return for ``pos = iso @ generate_grid(axes)`` -- the grid the
+    reference's ``Field.pre_pos`` builds for a structured mesh and
+    isometrizes (src/gstools/field/base.py:289-297,
+    src/gstools/tools/geometric.py:340-356, src/gstools/covmodel/base.py:
+    572-582) -- a float64 array of shape (n,) (scalar, Fourier) or (d, n)
+    (incompressible) in meshgrid "ij" order, without building that grid:
+    the wave vectors are mapped instead (``<k, M x> = <M^T k, x>``) and the
+    separable grid kernels run on the axis arrays.
+
+    * ``precision="f64"``: the FP64 grid kernel (reference operation order
+      per point, with the mapped wave vectors);
+    * ``precision="mixed"``: the tensor-core contraction on 2-D / 3-D grids
+      (the mixed pointwise grid kernel in 1-D).
+
+    ``cov_samples`` holds the wave vectors (the Fourier generator's
+    ``modes`` for ``kind="fourier"``, with ``spectrum_factor``).  Cases
+    :func:`structured_supported` rejects raise ``ValueError``.
+    """
+    prec = config.check_precision(precision)
+    cov = np.ascontiguousarray(cov_samples, dtype=np.float64)
+    if cov.ndim == 1:
+        cov = cov.reshape(1, -1)
+    dim = cov.shape[0]
+    if not structured_supported(kind, dim, prec, iso):
+        raise ValueError(f"no grid kernel for a {dim}-D {kind} sum in "
+                         f"{prec} with this isometrize map")
+    m = _iso_matrix(iso, dim)
+    kmap = np.ascontiguousarray(m.T @ cov)
+    axes = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in axes]
+    n = int(np.prod([a.size for a in axes]))
+    if kind == "scalar":
+        if prec == "f64":
+            out = summate_grid(kmap, z_1, z_2, axes, precision="f64",
+                               method="pointwise")
+        else:
+            out = summate_grid(kmap, z_1, z_2, axes, precision="mixed",
+                               method="auto", out_dtype=np.float64)
+        return out.reshape(n)
+    if kind == "incompr":
+        if prec == "f64":
+            out = summate_incompr_grid(cov, z_1, z_2, axes, precision="f64",
+                                       method="pointwise")
+        else:
+            out = summate_incompr_grid(kmap, z_1, z_2, axes, precision="mixed",
+                                       method="tensor", out_dtype=np.float64,
+                                       proj_cov=cov)
+        return out.reshape(dim, n)
+    if spectrum_factor is None:
+        raise ValueError("kind='fourier' needs spectrum_factor")
+    out = summate_fourier_grid(spectrum_factor, kmap, z_1, z_2, axes,
+                               out_dtype=np.float64)
+    return out.reshape(n)

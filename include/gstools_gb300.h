@@ -112,7 +112,8 @@ int gst_summate_fourier_f64(int dim, int64_t n_modes, int64_t n_pts,
  * Limits: n_modes <= 16384 (GST_ERR_TOO_LARGE beyond); the mode range is
  * split across CTAs only as far as the partial sums fit in 4 MiB, so small
  * point counts may run with less parallelism.  The first call on a device
- * looks up the array's device address (make it before any stream capture).
+ * looks up the array's device address (make it before any stream capture:
+ * a first call on a capturing stream returns GST_ERR_INVALID_ARGUMENT).
  * All calls share the array: calls that overlap on the GPU race and must be
  * serialised by the caller. */
 int gst_summate_f64_noalloc(int dim, int64_t n_modes, int64_t n_pts,

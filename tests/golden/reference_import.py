@@ -19,8 +19,12 @@ import numpy as np
 import sys
 import types
 
+# The reference's ``src`` directory: $GSTOOLS_REFERENCE_SRC, else a checkout
+# named ``reference`` beside this repository.
+_REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 REFERENCE_SRC = os.environ.get(
-    "GSTOOLS_REFERENCE_SRC", "/root/reference/src"
+    "GSTOOLS_REFERENCE_SRC",
+    os.path.join(os.path.dirname(_REPO), "reference", "src"),
 )
 
 

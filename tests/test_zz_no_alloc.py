@@ -4,9 +4,14 @@
 allocate device memory (hosts that reserve all GPU memory for their own pool,
 latency-critical loops that cannot pay for an allocator call).  Its scratch
 lives in a fixed device array inside the library and keeps the previous
-call's contents, so the test runs two different calls in a row and checks
-each against ``gst_summate_f64`` (which allocates its scratch per call)
-within the FP64 bar of the other tests: max|diff| <= 1e-12 * max|ref|.
+call's contents, so the test runs different calls in a row and checks each
+against ``gst_summate_f64`` (which allocates its scratch per call) and
+against the FP64 C oracle on a subsample of the points, within the FP64 bar
+of the other tests: max|diff| <= 1e-12 * max|ref|.  The cases cover the
+three ways the call splits its work: mode range split over CTAs with the
+partial sums in the fixed array (2000 x 50 000, 777 x 3001, 4096 x 150 000),
+and the full 16 384-mode table on 300 000 points, where the partial sums
+would not fit and the kernel writes straight to ``out`` (no split).
 
 This file is collected last so that a failure here cannot hide the other
 tests in a run that stops at the first failure.
@@ -53,11 +58,24 @@ def lib():
     return _native.load()
 
 
+def _oracle_check(arrays, got, stride):
+    """FP64 C oracle on every `stride`-th point."""
+    import oracle
+
+    cov, z1, z2, pos = (a.cpu().numpy() for a in arrays)
+    sub = np.ascontiguousarray(pos[:, ::stride])
+    ref = oracle.c_summate(cov, z1, z2, sub)
+    err = np.max(np.abs(got[::stride] - ref))
+    assert err <= F64_REL * np.max(np.abs(ref)), err
+
+
 def test_noalloc_matches_allocating_entry_point_twice(lib):
-    # two calls in a row with different sizes: the second must not see the
-    # first call's table or partial sums
-    for seed, dim, n_modes, n_pts in ((11, 3, 2000, 50_000),
-                                      (12, 2, 777, 3001)):
+    # calls in a row with different sizes: none may see the previous call's
+    # table or partial sums
+    for seed, dim, n_modes, n_pts, stride in ((11, 3, 2000, 50_000, 7),
+                                              (12, 2, 777, 3001, 1),
+                                              (14, 3, 16384, 300_000, 101),
+                                              (15, 2, 4096, 150_000, 37)):
         arrays = _case(seed, dim, n_modes, n_pts)
         rc_ref, ref = _call(lib, "gst_summate_f64", dim, arrays, n_modes,
                             n_pts)
@@ -66,6 +84,7 @@ def test_noalloc_matches_allocating_entry_point_twice(lib):
         assert rc_ref == 0 and rc == 0
         assert np.all(np.isfinite(got))
         assert np.max(np.abs(got - ref)) <= F64_REL * np.max(np.abs(ref))
+        _oracle_check(arrays, got, stride)
 
 
 def test_noalloc_rejects_too_many_modes(lib):
