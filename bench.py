@@ -1096,8 +1096,16 @@ def wl_ensemble(args, torch, gg, flush):
         args, "matern2d_ensemble512", work / t_batch / 1e9, t_batch,
         "fp32 + exact turn reduction",
         {"realizations": len(gens), "mode_points_per_step": work,
-         "total_points": int(sum(pts)), "total_modes": int(sum(modes)),
-         "tile_variant": bs.variant, "autotune_ms": tune},
+         "total_points": int(sum(pts)), "total_modes": int(sum(modes))},
+        autotune={"chosen_variant": bs.variant,
+                  "chosen_shape": dict(zip(("points_per_tile", "modes_per_stage",
+                                            "ctas_per_sm"),
+                                           gg.batched.VARIANT_SHAPES[bs.variant])),
+                  "candidates_ms": {str(k): v for k, v in tune.items()},
+                  "spread": (max(tune.values()) / min(tune.values())
+                             if tune else None),
+                  "chosen_over_variant0": (tune[0] / tune[bs.variant]
+                                           if tune and 0 in tune else None)},
         sequential_f64={"value": work / t_seq64 / 1e9, "unit": UNIT,
                         "ms": t_seq64 * 1e3, "calls": len(gens)},
         sequential_mixed={"value": work / t_seqmx / 1e9, "unit": UNIT,

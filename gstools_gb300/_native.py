@@ -77,6 +77,7 @@ SIGNATURES = {
     "gst_grid_tc_contract": (_c_int, [_c_int, _i64, _ptr, _ptr,
                                       ctypes.c_size_t, _ptr, _c_int, _dbl,
                                       _ptr]),
+    "gst_batch_variants": (_c_int, []),
     "gst_batch_workspace_size": (_c_int, [_c_int, _i64, _ptr, _ptr, _c_int,
                                           ctypes.POINTER(ctypes.c_size_t)]),
     "gst_batch_prepare": (_c_int, [_c_int, _i64, _ptr, _ptr, _c_int, _ptr,

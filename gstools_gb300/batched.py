@@ -9,9 +9,11 @@ in a single persistent kernel over a queue of (realization, point tile) work
 items (``gst_batch_*`` in include/gstools_gb300.h), replayed from a CUDA
 graph.
 
-The tile shape is chosen per ensemble shape by timing the kernel variants on
-the loaded data (:meth:`BatchedSummator.tune`); the choice is cached per shape
-for the process.
+The kernel shape -- points per work tile, modes per shared-memory stage and
+CTAs per SM, six compiled variants (``VARIANT_SHAPES``) -- is chosen per
+ensemble shape by timing every variant on the loaded data
+(:meth:`BatchedSummator.tune`); the choice and the timings are cached per
+shape for the process.
 
 The modes can also be drawn on the device (:meth:`BatchedSummator.sample`):
 all realizations' amplitudes, directions and radii in one launch from a
@@ -33,7 +35,17 @@ from .summator import device
 
 __all__ = ["BatchedSummator", "VARIANTS"]
 
-VARIANTS = (0, 1)  # 512 or 1024 points per work tile
+# (points per work tile, modes per stage, CTAs per SM) of each compiled
+# variant of the persistent kernel (gst_batched.cu)
+VARIANT_SHAPES = {
+    0: (512, 256, 2),
+    1: (1024, 256, 2),
+    2: (512, 256, 3),
+    3: (512, 128, 3),
+    4: (256, 256, 4),
+    5: (1024, 128, 2),
+}
+VARIANTS = tuple(VARIANT_SHAPES)
 
 _tune_cache = {}
 _tune_lock = threading.Lock()
@@ -92,6 +104,7 @@ class BatchedSummator:
         self._points_c = self.points.ctypes.data_as(ctypes.c_void_p)
         self.use_graph = bool(graph)
         self.variant = None
+        self.timings = {}
         self.workspace = None
         self.ws_bytes = ctypes.c_size_t(0)
         self._graph = None
@@ -218,32 +231,38 @@ class BatchedSummator:
                      _ptr(self.z2), _ptr(self.pos), _ptr(self.scales),
                      _ptr(self.out), self.out_code, _ptr(ws), nbytes, stream)
 
-    def tune(self, repeats=3):
-        """Time every tile variant on the loaded data; keep the fastest."""
+    def tune(self, repeats=3, variants=None):
+        """Time every kernel variant on the loaded data (best of ``repeats``
+        runs after one warm-up, CUDA events) and keep the fastest; returns
+        ``{variant: ms}`` (the cached timings when this ensemble shape was
+        tuned before in this process)."""
         with _tune_lock:
             cached = _tune_cache.get(self.key)
-        timings = {}
         if cached is None:
-            for v in VARIANTS:
+            timings = {}
+            stream = torch.cuda.current_stream(self.dev)
+            for v in (VARIANTS if variants is None else variants):
                 ws, nbytes = self._prepare(v)
                 self._launch(v, ws, nbytes)  # warm-up
                 best = float("inf")
                 for _ in range(repeats):
                     e0 = torch.cuda.Event(enable_timing=True)
                     e1 = torch.cuda.Event(enable_timing=True)
-                    e0.record()
+                    e0.record(stream)
                     self._launch(v, ws, nbytes)
-                    e1.record()
+                    e1.record(stream)
                     e1.synchronize()
                     best = min(best, e0.elapsed_time(e1))
                 timings[v] = best
-            cached = min(timings, key=timings.get)
+                del ws
+            cached = (min(timings, key=timings.get), timings)
             with _tune_lock:
                 _tune_cache[self.key] = cached
-        self.variant = cached
+        self.variant, timings = cached
+        self.timings = dict(timings)
         self.workspace, self.ws_bytes = self._prepare(self.variant)
         self._graph = None
-        return timings
+        return dict(timings)
 
     def _capture(self):
         side = torch.cuda.Stream(self.dev)

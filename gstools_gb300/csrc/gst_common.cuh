@@ -46,6 +46,17 @@ cudaMemPool_t scratch_pool();
 // that overlap the library's kernels (created on first use), or null.
 cudaStream_t copy_stream();
 
+// Mixed-precision summate of one unstructured point set (gst_batched.cu):
+// points sorted spatially and modes by |k|_1, amplitude-phase form, per-warp
+// origins; out (n_pts) float32 (out_f32) or float64, scaled by `scale`.
+int summate_mixed_sorted(int dim, int64_t n_modes, int64_t n_pts, const double *cov,
+                         const double *z1, const double *z2, const double *pos,
+                         void *out, int out_f32, double scale, cudaStream_t s);
+// When gst_summate_mixed takes that path: at least this many mode-points and
+// at most this many modes.
+constexpr double kSortedMinWork = 1e9;
+constexpr int64_t kSortedMaxModes = 16384;
+
 // Stream-ordered scratch allocation that always frees on the same stream.
 struct StreamScratch {
     void *ptr = nullptr;

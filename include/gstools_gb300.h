@@ -130,7 +130,10 @@ int gst_summate_f64_noalloc(int dim, int64_t n_modes, int64_t n_pts,
 /* ----------------------------------------------------------------------- */
 
 /* Same contract as gst_summate_f64; `out` is double (GST_OUT_F64) or float
- * (GST_OUT_F32).  dim in 1..3. */
+ * (GST_OUT_F32).  dim in 1..3.  Sums of at least 1e9 mode-points with at
+ * most 16384 modes run the sorted amplitude-phase path of the ensembles
+ * (points sorted spatially, modes by |k|_1, one SFU cosine per mode and
+ * point); smaller ones the pointwise kernel described above. */
 int gst_summate_mixed(int dim, int64_t n_modes, int64_t n_pts,
                       const double *cov_samples, const double *z_1,
                       const double *z_2, const double *pos, void *out,
@@ -281,12 +284,21 @@ int gst_summate_vjp_pos_mixed(int dim, int64_t n_modes, int64_t n_pts,
 /* (dim, total_points) and out (total_points,).  mode_counts and            */
 /* point_counts are HOST arrays; scales (device, n_items, may be NULL)      */
 /* multiplies each realization's result (sqrt(var_r / N_r) for RandMeth).   */
-/* Arithmetic: the mixed-precision path.  variant selects the tile shape    */
-/* (0: 512 points per tile, 1: 1024).  gst_batch_prepare (synchronous, once */
-/* per ensemble shape) writes the work list into the caller's workspace;   */
-/* gst_batch_run is asynchronous, allocates nothing and may be captured in  */
-/* a CUDA graph; it must see the same counts and variant as prepare.        */
+/* Arithmetic: mixed precision in amplitude-phase form (one SFU cosine per  */
+/* mode and point); each realization's points are sorted spatially and its  */
+/* modes by |k|_1 inside gst_batch_run, so that compact work tiles run the  */
+/* phase in plain FP32 where |<k, x - x_warp>| stays small and the exact    */
+/* split turn reduction elsewhere.  variant (0 .. gst_batch_variants() - 1) */
+/* selects the kernel shape: points per tile, modes per shared-memory stage */
+/* and CTAs per SM (0: 512/256/2, 1: 1024/256/2, 2: 512/256/3,             */
+/* 3: 512/128/3, 4: 256/256/4, 5: 1024/128/2).  gst_batch_prepare           */
+/* (synchronous, once per ensemble shape and variant) writes the work list  */
+/* into the caller's workspace; gst_batch_run is asynchronous, allocates    */
+/* nothing and may be captured in a CUDA graph; it must see the same counts */
+/* and variant as prepare.  gst_batch_variants has no counterpart in the    */
+/* reference: the number of compiled kernel shapes.                         */
 /* ----------------------------------------------------------------------- */
+int gst_batch_variants(void);
 int gst_batch_workspace_size(int dim, int64_t n_items, const int64_t *mode_counts,
                              const int64_t *point_counts, int variant,
                              size_t *bytes);
