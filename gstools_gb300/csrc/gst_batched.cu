@@ -68,6 +68,7 @@ constexpr int kChunk = 32;          // modes per |k|_1 maximum (one warp pass)
 constexpr int kModeBuckets = 128;
 constexpr int kPackThreads = 256;
 constexpr int kSortThreads = 1024;
+constexpr int kScatterThreads = 512;
 constexpr int kCells = 4096;        // Morton cells of the point sort
 constexpr int kSegPoints = 4096;    // points per sort segment
 // Largest |<k, x''>| (radians) a fast chunk may see: the FP32 phase error
@@ -237,7 +238,8 @@ __device__ void write_entry(float *e, int dim, const double *cov,
 
 // One CTA per realization: stable bucket sort of its modes by |k|_1, the
 // table entries in that order (zero entries up to the stage padding), and
-// the largest FP32 |k|_1 of every 32-entry chunk.
+// the largest FP32 |k|_1 of every 32-entry chunk (zeroed first, then raised
+// by every entry written; the CTA's barriers order the zeroing before).
 __global__ void __launch_bounds__(kPackThreads)
     pack_batch_kernel(int dim, const Item *__restrict__ items, int64_t total_modes,
                       const double *__restrict__ cov, const double *__restrict__ z1,
@@ -252,7 +254,9 @@ __global__ void __launch_bounds__(kPackThreads)
     const double x0[3] = {item_origin(pos, total_pts, it, 0, dim),
                           item_origin(pos, total_pts, it, 1, dim),
                           item_origin(pos, total_pts, it, 2, dim)};
+    float *kmax_r = kmax + it.table_off / kChunk;   // this realization's chunks
     for (int b = tid; b < kModeBuckets; b += kPackThreads) hist[b] = 0u;
+    for (int64_t c = tid; c < padded / kChunk; c += kPackThreads) kmax_r[c] = 0.0f;
     __syncthreads();
     for (int64_t j = tid; j < it.n_modes; j += kPackThreads)
         atomicAdd(&hist[mode_bucket(mode_key(dim, cov, total_modes, it.mode_off + j))], 1u);
@@ -295,22 +299,18 @@ __global__ void __launch_bounds__(kPackThreads)
         }
         if (valid) {
             const unsigned dst = s_base[warp * 32 + leader] + rank;
-            write_entry(base_e + static_cast<int64_t>(dst) * kEntryFloats, dim, cov,
-                        total_modes, it.mode_off + j, z1, z2, x0);
+            float *e = base_e + static_cast<int64_t>(dst) * kEntryFloats;
+            write_entry(e, dim, cov, total_modes, it.mode_off + j, z1, z2, x0);
+            // the chunk maximum of the FP32 |k|_1 (non-negative floats order
+            // like their bit patterns, so an integer maximum; order-free)
+            const float k1 = fabsf(e[0]) + fabsf(e[1]) + fabsf(e[2]);
+            atomicMax(reinterpret_cast<int *>(kmax_r + dst / kChunk), __float_as_int(k1));
         }
         __syncthreads();
     }
     for (int64_t j = it.n_modes + tid; j < padded; j += kPackThreads) {
         float *e = base_e + j * kEntryFloats;
         for (int i = 0; i < kEntryFloats; ++i) e[i] = 0.0f;
-    }
-    __syncthreads();
-    for (int64_t c = tid; c < padded / kChunk; c += kPackThreads) {
-        const float *e = base_e + c * kChunk * kEntryFloats;
-        float m = 0.0f;
-        for (int i = 0; i < kChunk; ++i, e += kEntryFloats)
-            m = fmaxf(m, fabsf(e[0]) + fabsf(e[1]) + fabsf(e[2]));
-        kmax[it.table_off / kChunk + c] = m;
     }
 }
 
@@ -387,20 +387,28 @@ __global__ void __launch_bounds__(256)
 }
 
 // The realization's bounding box from its segments' boxes, and the cell
-// scale of every axis.
-__device__ __forceinline__ void item_cells(int dim, const Item &it, const double *box,
-                                           double (&lo)[3], double (&inv)[3]) {
+// scale of every axis, into s_lo / s_inv: computed by one whole warp (lanes
+// stride over the segments), lane 0 stores.
+__device__ __forceinline__ void item_cells_warp(int dim, const Item &it, const double *box,
+                                                double *s_lo, double *s_inv) {
+    const int lane = threadIdx.x & 31;
     const int cpa = cells_per_axis(dim);
     for (int d = 0; d < 3; ++d) {
         double l = INFINITY, h = -INFINITY;
         if (d < dim)
-            for (int64_t s = 0; s < it.n_seg; ++s) {
+            for (int64_t s = lane; s < it.n_seg; s += 32) {
                 l = fmin(l, box[(it.seg_off + s) * 6 + d]);
                 h = fmax(h, box[(it.seg_off + s) * 6 + 3 + d]);
             }
+        for (int o = 16; o > 0; o >>= 1) {
+            l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
+            h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+        }
         const double ext = h - l;
-        lo[d] = l;
-        inv[d] = (d < dim && ext > 0.0 && isfinite(ext)) ? cpa / ext : 0.0;
+        if (lane == 0) {
+            s_lo[d] = l;
+            s_inv[d] = (d < dim && ext > 0.0 && isfinite(ext)) ? cpa / ext : 0.0;
+        }
     }
 }
 
@@ -426,14 +434,7 @@ __global__ void __launch_bounds__(kSortThreads)
     __shared__ double s_lo[3], s_inv[3];
     const Seg sg = seg_of(segs, blockIdx.x);
     const Item it = items[sg.item];
-    if (threadIdx.x == 0) {
-        double lo[3], inv[3];
-        item_cells(dim, it, box, lo, inv);
-        for (int d = 0; d < 3; ++d) {
-            s_lo[d] = lo[d];
-            s_inv[d] = inv[d];
-        }
-    }
+    if (threadIdx.x < 32) item_cells_warp(dim, it, box, s_lo, s_inv);
     for (int c = threadIdx.x; c < kCells; c += kSortThreads) h[c] = 0u;
     __syncthreads();
     const double lo[3] = {s_lo[0], s_lo[1], s_lo[2]};
@@ -501,30 +502,23 @@ __global__ void __launch_bounds__(kSortThreads)
 }
 
 // Segment blockIdx.x scatters its points in order (warps in turn within each
-// chunk of kSortThreads points): a stable sort.  Coordinates relative to
+// chunk of kScatterThreads points): a stable sort.  Coordinates relative to
 // the realization's first point; perm holds each sorted slot's point index
 // within its realization.
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kScatterThreads)
     seg_scatter_kernel(int dim, const Item *__restrict__ items, const Seg *__restrict__ segs,
                        const double *__restrict__ pos, int64_t total_pts,
                        const double *__restrict__ box, const unsigned *__restrict__ hist,
                        double *__restrict__ sorted, int32_t *__restrict__ perm) {
     __shared__ unsigned cur[kCells];
-    __shared__ unsigned s_base[kSortThreads];
+    __shared__ unsigned s_base[kScatterThreads];
     __shared__ double s_lo[3], s_inv[3];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const Seg sg = seg_of(segs, blockIdx.x);
     const Item it = items[sg.item];
-    if (tid == 0) {
-        double lo[3], inv[3];
-        item_cells(dim, it, box, lo, inv);
-        for (int d = 0; d < 3; ++d) {
-            s_lo[d] = lo[d];
-            s_inv[d] = inv[d];
-        }
-    }
+    if (tid < 32) item_cells_warp(dim, it, box, s_lo, s_inv);
     const unsigned *src = hist + static_cast<int64_t>(blockIdx.x) * kCells;
-    for (int c = tid; c < kCells; c += kSortThreads) cur[c] = src[c];
+    for (int c = tid; c < kCells; c += kScatterThreads) cur[c] = src[c];
     __syncthreads();
     const double lo[3] = {s_lo[0], s_lo[1], s_lo[2]};
     const double inv[3] = {s_inv[0], s_inv[1], s_inv[2]};
@@ -532,7 +526,7 @@ __global__ void __launch_bounds__(kSortThreads)
     for (int d = 0; d < 3; ++d) x0[d] = item_origin(pos, total_pts, it, d, dim);
     const double *p0 = pos + it.pt_off;
     const int64_t i1 = min(sg.begin + kSegPoints, it.n_pts);
-    for (int64_t c0 = sg.begin; c0 < i1; c0 += kSortThreads) {
+    for (int64_t c0 = sg.begin; c0 < i1; c0 += kScatterThreads) {
         const int64_t i = c0 + tid;
         const bool valid = i < i1;
         const unsigned key = valid ? point_cell(dim, p0 + i, total_pts, lo, inv)
@@ -540,7 +534,7 @@ __global__ void __launch_bounds__(kSortThreads)
         const unsigned peers = __match_any_sync(0xffffffffu, key);
         const int leader = __ffs(peers) - 1;
         const unsigned rank = __popc(peers & lanemask_lt());
-        for (int w = 0; w < kSortThreads / 32; ++w) {   // warps in order
+        for (int w = 0; w < kScatterThreads / 32; ++w) {   // warps in order
             if (warp == w && valid && lane == leader) {
                 s_base[tid] = cur[key];
                 cur[key] += __popc(peers);
@@ -929,8 +923,8 @@ cudaError_t run_prologue(int dim, int64_t n_items, const Item *items, int64_t n_
                                                   hist);
         cell_scan_kernel<<<static_cast<unsigned>(n_items), kSortThreads, 0, s>>>(items,
                                                                                 hist);
-        seg_scatter_kernel<<<g, kSortThreads, 0, s>>>(dim, items, segs, pos, total_pts, box,
-                                                     hist, sorted, perm);
+        seg_scatter_kernel<<<g, kScatterThreads, 0, s>>>(dim, items, segs, pos, total_pts,
+                                                        box, hist, sorted, perm);
     }
     return cudaGetLastError();
 }
