@@ -71,8 +71,8 @@ VAR = 2.0
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 # DRAM bytes (read + write) of one contraction launch on this workload
 # (dram__bytes_read.sum + dram__bytes_write.sum of grid_tc_kernel, one ncu
-# capture of this build).
-TC_DRAM_BYTES_PER_LAUNCH = 34.6e6
+# capture of this build: 20.2 MB + 14.5 MB).
+TC_DRAM_BYTES_PER_LAUNCH = 34.7e6
 
 
 def parse():
@@ -640,7 +640,9 @@ def run_ours(args):
                 "unit": "TFLOP/s", "frac": alg / peak,
                 "traffic": TC_DRAM_BYTES_PER_LAUNCH,
                 "traffic_note": ("dram read+write bytes per contraction "
-                                 "launch (ncu full capture of this build); "
+                                 "launch, from one ncu --set full capture of "
+                                 "this build on this workload (a constant: "
+                                 "no counter is read during a timed run); "
                                  "the 67 MB float32 field stays in L2 at "
                                  "launch end"),
                 "kernel": "grid_tc_kernel (contraction)",

@@ -208,8 +208,8 @@ __device__ __forceinline__ double mode_key(int dim, const double *cov,
 // k in FP32 (radians per unit, the fast path), q = k / 2 pi split into a
 // 12-significant-bit head and an FP32 tail (the exact path), A = hypot(z1,
 // z2), psi0 = atan2(z2, z1) / 2 pi - <q, x0> reduced to [-1/2, 1/2]: the
-// dot product and its reduction in FP64, atan2 in FP32 (its result is
-// rounded to FP32 in the table anyway).
+// dot product and its reduction in FP64, atan2 and hypot in FP32 (their
+// results are rounded to FP32 in the table anyway).
 __device__ void write_entry(float *e, int dim, const double *cov,
                             int64_t total_modes, int64_t m, const double *z1,
                             const double *z2, const double (&x0)[3]) {
@@ -231,7 +231,7 @@ __device__ void write_entry(float *e, int dim, const double *cov,
         e[4 + d] = qh;
         e[8 + d] = static_cast<float>(q - static_cast<double>(qh));
     }
-    e[3] = static_cast<float>(hypot(a1, a2));
+    e[3] = hypotf(static_cast<float>(a1), static_cast<float>(a2));
     e[7] = static_cast<float>(psi);
     for (int d = 11; d < 16; ++d) e[d] = 0.0f;
 }
