@@ -31,7 +31,7 @@ import numpy as np
 import torch
 
 from . import _native
-from .summator import device
+from .summator import _finish, device
 
 __all__ = ["BatchedSummator", "VARIANTS"]
 
@@ -105,6 +105,8 @@ class BatchedSummator:
         self.use_graph = bool(graph)
         self.variant = None
         self.timings = {}
+        self._stage = {}      # page-locked host staging buffers of load()
+        self._staged = None   # event: the last uploads from them are done
         self.workspace = None
         self.ws_bytes = ctypes.c_size_t(0)
         self._graph = None
@@ -112,19 +114,44 @@ class BatchedSummator:
                                            + self.points.tobytes()).hexdigest())
 
     # -- data -------------------------------------------------------------
-    def load_points(self, pos):
-        """Copy the per-realization point sets (already isometrized, the
-        reference's (dim, n) layout) into the device buffer."""
-        if len(pos) != self.n_items:
-            raise ValueError("one point set per realization expected")
-        xx = np.zeros((self.dim, self.total_points))
+    def _staging(self, name, shape):
+        """A page-locked host buffer of this summator (allocated once), free
+        to overwrite: the copies issued from it by the previous load have
+        completed."""
+        if self._staged is not None:
+            self._staged.synchronize()
+            self._staged = None
+        buf = self._stage.get(name)
+        if buf is None:
+            buf = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+            self._stage[name] = buf
+        return buf
+
+    def _upload(self, pairs):
+        """Asynchronous copies host staging -> device, then an event that
+        the next load waits for before it refills the staging buffers."""
+        stream = torch.cuda.current_stream(self.dev)
+        for dst, src in pairs:
+            dst.copy_(src, non_blocking=True)
+        self._staged = torch.cuda.Event()
+        self._staged.record(stream)
+
+    def _fill_points(self, pos, xx):
         for r in range(self.n_items):
             p0, p1 = self.point_off[r], self.point_off[r + 1]
             x = np.asarray(pos[r], dtype=np.float64).reshape(self.dim, -1)
             if x.shape[1] != p1 - p0:
                 raise ValueError(f"realization {r}: sizes do not match the plan")
             xx[:, p0:p1] = x
-        self.pos.copy_(torch.from_numpy(xx).pin_memory(), non_blocking=True)
+
+    def load_points(self, pos):
+        """Copy the per-realization point sets (already isometrized, the
+        reference's (dim, n) layout) into the device buffer."""
+        if len(pos) != self.n_items:
+            raise ValueError("one point set per realization expected")
+        xx = self._staging("pos", (self.dim, self.total_points))
+        self._fill_points(pos, xx.numpy())
+        self._upload([(self.pos, xx)])
 
     def sample(self, model, seeds, len_scales=None, variances=None):
         """Draw every realization's modes on the device (asynchronous).
@@ -178,24 +205,22 @@ class BatchedSummator:
         if not (len(cov_samples) == len(z_1) == len(z_2) == len(pos)
                 == self.n_items):
             raise ValueError("one array per realization expected")
-        cov = np.zeros((self.dim, self.total_modes))
-        zz1 = np.zeros(self.total_modes)
-        zz2 = np.zeros(self.total_modes)
-        xx = np.zeros((self.dim, self.total_points))
+        cov_h = self._staging("cov", (self.dim, self.total_modes))
+        z1_h = self._staging("z1", (self.total_modes,))
+        z2_h = self._staging("z2", (self.total_modes,))
+        xx_h = self._staging("pos", (self.dim, self.total_points))
+        cov, zz1, zz2 = cov_h.numpy(), z1_h.numpy(), z2_h.numpy()
         for r in range(self.n_items):
             m0, m1 = self.mode_off[r], self.mode_off[r + 1]
-            p0, p1 = self.point_off[r], self.point_off[r + 1]
             c = np.asarray(cov_samples[r], dtype=np.float64).reshape(self.dim, -1)
-            x = np.asarray(pos[r], dtype=np.float64).reshape(self.dim, -1)
-            if c.shape[1] != m1 - m0 or x.shape[1] != p1 - p0:
+            if c.shape[1] != m1 - m0:
                 raise ValueError(f"realization {r}: sizes do not match the plan")
             cov[:, m0:m1] = c
             zz1[m0:m1] = np.asarray(z_1[r], dtype=np.float64).reshape(-1)
             zz2[m0:m1] = np.asarray(z_2[r], dtype=np.float64).reshape(-1)
-            xx[:, p0:p1] = x
-        for dst, src in ((self.cov, cov), (self.z1, zz1), (self.z2, zz2),
-                         (self.pos, xx)):
-            dst.copy_(torch.from_numpy(src).pin_memory(), non_blocking=True)
+        self._fill_points(pos, xx_h.numpy())
+        self._upload([(self.cov, cov_h), (self.z1, z1_h), (self.z2, z2_h),
+                      (self.pos, xx_h)])
         if scales is not None:
             s = np.asarray(scales, dtype=np.float64).reshape(-1)
             if s.size != self.n_items:
@@ -205,8 +230,10 @@ class BatchedSummator:
             self.scales.fill_(1.0)
 
     def split(self, out=None):
-        """Per-realization numpy views of a host copy of ``out``."""
-        host = (self.out if out is None else out).cpu().numpy()
+        """Per-realization numpy views of a host copy of ``out`` (a pooled
+        page-locked buffer that the returned arrays keep alive)."""
+        src = self.out if out is None else out
+        host = _finish(src, False)
         return [host[self.point_off[r]:self.point_off[r + 1]]
                 for r in range(self.n_items)]
 

@@ -28,7 +28,13 @@ from . import _native, config
 from .summator import _p, _stream, device
 
 __all__ = ["SummateFunction", "summate_torch", "isometrize_matrix",
-           "randmeth_field"]
+           "randmeth_field", "SPARSE_COTANGENT"]
+
+# Run the adjoint kernels on the points with a nonzero cotangent only, when
+# at most a quarter of the points have one (read at every backward).  The
+# gradients are the same sums; points whose cotangent is zero are left out,
+# so a non-finite coordinate there no longer turns the mode gradients NaN.
+SPARSE_COTANGENT = True
 
 
 def _dev_f64(t, dev):
@@ -68,21 +74,38 @@ class SummateFunction(torch.autograd.Function):
         stream = _stream(dev)
         need_cov, need_z1, need_z2, need_pos = ctx.needs_input_grad[:4]
         d_cov = d_z1 = d_z2 = d_pos = None
+        # Points whose cotangent is exactly zero add nothing to the mode
+        # gradients and get a zero position gradient; when at most a quarter
+        # of the points carry one (a loss on a subset of the field) the
+        # adjoint kernels run on those points only.
+        idx = None
+        if SPARSE_COTANGENT and n_pts > 0:
+            nnz = int(torch.count_nonzero(g))
+            if 4 * nnz <= n_pts:
+                idx = torch.nonzero(g).reshape(-1)
+        xs, gs = (x, g) if idx is None else (x.index_select(1, idx).contiguous(),
+                                             g.index_select(0, idx).contiguous())
+        n_sel = xs.shape[1]
         if need_cov or need_z1 or need_z2:
             gz1 = torch.empty(n_modes, dtype=torch.float64, device=dev)
             gz2 = torch.empty(n_modes, dtype=torch.float64, device=dev)
             gk = torch.empty((dim, n_modes), dtype=torch.float64, device=dev)
             _native.call(f"gst_summate_vjp_modes_{ctx.prec}", dim, n_modes,
-                         n_pts, _p(cov), _p(z1), _p(z2), _p(x), _p(g),
+                         n_sel, _p(cov), _p(z1), _p(z2), _p(xs), _p(gs),
                          _p(gz1), _p(gz2), _p(gk), stream)
             d_cov = gk.to(ctx.in_devices[0]) if need_cov else None
             d_z1 = gz1.to(ctx.in_devices[1]) if need_z1 else None
             d_z2 = gz2.to(ctx.in_devices[2]) if need_z2 else None
         if need_pos:
-            v = torch.empty((dim, n_pts), dtype=torch.float64, device=dev)
+            v = torch.empty((dim, n_sel), dtype=torch.float64, device=dev)
             _native.call(f"gst_summate_vjp_pos_{ctx.prec}", dim, n_modes,
-                         n_pts, _p(cov), _p(z1), _p(z2), _p(x), _p(v), stream)
-            d_pos = (v * g).to(ctx.in_devices[3])
+                         n_sel, _p(cov), _p(z1), _p(z2), _p(xs), _p(v), stream)
+            if idx is None:
+                d_pos = v * g
+            else:
+                d_pos = torch.zeros((dim, n_pts), dtype=torch.float64, device=dev)
+                d_pos.index_copy_(1, idx, v * gs)
+            d_pos = d_pos.to(ctx.in_devices[3])
         return d_cov, d_z1, d_z2, d_pos, None
 
 

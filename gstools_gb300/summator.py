@@ -68,23 +68,54 @@ def _is_torch(*arrays):
     return any(isinstance(a, torch.Tensor) for a in arrays)
 
 
+def _upload_host(arrays, dev):
+    """Host arrays as float64 device tensors through ONE asynchronous copy
+    from a pooled page-locked block (instead of a pageable copy each).
+    Returns the tensors and the block, which the caller keeps referenced
+    until its stream has passed the copy (``_finish`` synchronises)."""
+    flat = [np.ascontiguousarray(a, dtype=np.float64) for a in arrays]
+    total = sum(f.size for f in flat)
+    if total * 8 < _PINNED_MIN_BYTES:
+        return [torch.from_numpy(f).to(dev) for f in flat], None
+    block = _PinnedBlock(total * 8)
+    host = block.tensor.view(torch.float64)
+    host_np = host.numpy()
+    off = 0
+    for f in flat:
+        host_np[off:off + f.size] = f.reshape(-1)
+        off += f.size
+    dbuf = torch.empty(total, dtype=torch.float64, device=dev)
+    dbuf.copy_(host, non_blocking=True)
+    out, off = [], 0
+    for f in flat:
+        out.append(dbuf[off:off + f.size].view(f.shape))
+        off += f.size
+    return out, block
+
+
 def _prepare(cov_samples, z_1, z_2, pos):
+    """Validated float64 device tensors of the inputs, and an object the
+    caller keeps referenced until the result is synchronised (the staging
+    block of host inputs, or None)."""
     dev = device()
-    cov = _on_device(cov_samples, dev)
+    keep = None
+    if _is_torch(cov_samples, z_1, z_2, pos):
+        cov, z1, z2, x = (_on_device(a, dev) for a in (cov_samples, z_1, z_2, pos))
+    else:
+        (cov, z1, z2, x), keep = _upload_host((cov_samples, z_1, z_2, pos), dev)
     if cov.dim() == 1:
         cov = cov.reshape(1, -1)
     if cov.dim() != 2:
         raise ValueError("cov_samples must have shape (dim, N)")
     dim, n_modes = cov.shape
-    z1 = _on_device(z_1, dev).reshape(-1)
-    z2 = _on_device(z_2, dev).reshape(-1)
+    z1 = z1.reshape(-1)
+    z2 = z2.reshape(-1)
     if z1.numel() != n_modes or z2.numel() != n_modes:
         raise ValueError("z_1 and z_2 must have N = cov_samples.shape[1] values")
-    x = _on_device(pos, dev)
     if x.numel() % max(dim, 1):
         raise ValueError("pos must have shape (dim, n)")
     x = x.reshape(dim, -1)
-    return dev, cov, z1, z2, x
+    return dev, cov, z1, z2, x, keep
 
 
 _PINNED_MIN_BYTES = 1 << 20
@@ -170,7 +201,7 @@ def summate(cov_samples, z_1, z_2, pos, num_threads=None, *, precision=None,
     """
     prec = config.check_precision(precision)
     as_torch = _is_torch(cov_samples, z_1, z_2, pos)
-    dev, cov, z1, z2, x = _prepare(cov_samples, z_1, z_2, pos)
+    dev, cov, z1, z2, x, keep = _prepare(cov_samples, z_1, z_2, pos)
     dim, n_modes = cov.shape
     n_pts = x.shape[1]
     stream = _stream(dev)
@@ -185,7 +216,9 @@ def summate(cov_samples, z_1, z_2, pos, num_threads=None, *, precision=None,
         out = _output((n_pts,), tdtype, dev, as_torch)
         _native.call("gst_summate_mixed", dim, n_modes, n_pts, _p(cov),
                      _p(z1), _p(z2), _p(x), _p(out), code, stream)
-    return _finish(out, as_torch)
+    result = _finish(out, as_torch)
+    del keep   # the staged inputs are no longer read
+    return result
 
 
 def summate_incompr(cov_samples, z_1, z_2, pos, num_threads=None, *,
@@ -197,7 +230,7 @@ def summate_incompr(cov_samples, z_1, z_2, pos, num_threads=None, *,
     """
     prec = config.check_precision(precision)
     as_torch = _is_torch(cov_samples, z_1, z_2, pos)
-    dev, cov, z1, z2, x = _prepare(cov_samples, z_1, z_2, pos)
+    dev, cov, z1, z2, x, keep = _prepare(cov_samples, z_1, z_2, pos)
     dim, n_modes = cov.shape
     n_pts = x.shape[1]
     stream = _stream(dev)
@@ -210,7 +243,9 @@ def summate_incompr(cov_samples, z_1, z_2, pos, num_threads=None, *,
         out = torch.empty((dim, n_pts), dtype=tdtype, device=dev)
         _native.call("gst_summate_incompr_mixed", dim, n_modes, n_pts,
                      _p(cov), _p(z1), _p(z2), _p(x), _p(out), code, stream)
-    return _finish(out, as_torch)
+    result = _finish(out, as_torch)
+    del keep   # the staged inputs are no longer read
+    return result
 
 
 def summate_fourier(spectrum_factor, modes, z_1, z_2, pos, num_threads=None):
@@ -219,7 +254,7 @@ def summate_fourier(spectrum_factor, modes, z_1, z_2, pos, num_threads=None):
     ``out[i] = sum_j f[j] (z_1[j] cos(<k_j, x_i>) + z_2[j] sin(<k_j, x_i>))``.
     """
     as_torch = _is_torch(spectrum_factor, modes, z_1, z_2, pos)
-    dev, kk, z1, z2, x = _prepare(modes, z_1, z_2, pos)
+    dev, kk, z1, z2, x, keep = _prepare(modes, z_1, z_2, pos)
     fac = _on_device(spectrum_factor, dev).reshape(-1)
     dim, n_modes = kk.shape
     if fac.numel() != n_modes:
@@ -228,7 +263,9 @@ def summate_fourier(spectrum_factor, modes, z_1, z_2, pos, num_threads=None):
     out = torch.empty(n_pts, dtype=torch.float64, device=dev)
     _native.call("gst_summate_fourier_f64", dim, n_modes, n_pts, _p(fac),
                  _p(kk), _p(z1), _p(z2), _p(x), _p(out), _stream(dev))
-    return _finish(out, as_torch)
+    result = _finish(out, as_torch)
+    del keep   # the staged inputs are no longer read
+    return result
 
 
 def _prepare_grid(cov_samples, z_1, z_2, axes):

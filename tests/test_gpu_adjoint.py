@@ -133,3 +133,33 @@ def test_vjp_empty_points(cuda_lib):
     out = summate_torch(cov, z1, z2, pos, "f64")
     out.sum().backward()
     assert torch.all(cov.grad == 0) and torch.all(z1.grad == 0)
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-12), ("mixed", 1e-5)])
+def test_sparse_cotangent_matches_all_points(cuda_lib, precision, tol):
+    """A loss on 1 % of the points: the backward that runs the adjoint
+    kernels on the points with a nonzero cotangent only gives the gradients
+    of the backward over all points (same terms, other summation order)."""
+    from gstools_gb300 import grad
+
+    cov, z1, z2, pos, _ = leaves(21, 3, 700, 40_000)
+    obs = torch.arange(0, 40_000, 97, device="cuda")
+    target = torch.randn(obs.numel(), dtype=torch.float64, device="cuda")
+    results = {}
+    for sparse in (True, False):
+        grad.SPARSE_COTANGENT = sparse
+        try:
+            for t in (cov, z1, z2, pos):
+                t.grad = None
+            u = summate_torch(cov, z1, z2, pos, precision)
+            torch.mean((u[obs] - target) ** 2).backward()
+            results[sparse] = [t.grad.clone() for t in (cov, z1, z2, pos)]
+        finally:
+            grad.SPARSE_COTANGENT = True
+    for name, a, b in zip(("cov", "z1", "z2", "pos"), results[True],
+                          results[False]):
+        assert rel(a, b) <= tol, (name, rel(a, b))
+    # positions off the observation set get exactly zero
+    mask = torch.ones(40_000, dtype=torch.bool, device="cuda")
+    mask[obs] = False
+    assert torch.all(results[True][3][:, mask] == 0)
