@@ -797,7 +797,7 @@ __global__ void __launch_bounds__(kThreads, CTAS) batched_kernel(const BatchArgs
                 const float4 *ek = reinterpret_cast<const float4 *>(e) +
                                    c * kChunk * (kEntryFloats / 4);
                 if (__shfl_sync(0xffffffffu, kmax_lane, c) * half <= kFastBound) {
-#pragma unroll 4
+#pragma unroll 8
                     for (int j = c * kChunk; j < (c + 1) * kChunk;
                          ++j, ek += kEntryFloats / 4) {
                         const float4 kk = ek[0];   // k0 k1 k2 A
