@@ -82,6 +82,11 @@ def parse():
                    help="timed steps (default 200 for the headline grid, "
                         "10 for the other workloads)")
     p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--min-timed-s", dest="min_timed_s", type=float, default=0.25,
+                   help="other workloads: the timed steps of the measurement "
+                        "behind `value` go on until they span this many "
+                        "seconds (at least --steps), so that the clock "
+                        "samples fall inside the timed region")
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--grid", type=int, default=GRID)
     p.add_argument("--path", default="auto",
@@ -713,12 +718,23 @@ def run_ours(args):
 # Each prints one JSON line with the same timing rules.
 # ---------------------------------------------------------------------------
 
-def _timed_events(torch, fn, steps, warmup, flush):
+# The timed region of the measurement a workload line's `value` comes from:
+# host window (for the clock record) and the number of timed steps.
+_MAIN = {"window": None, "steps": 0}
+
+
+def _timed_events(torch, fn, steps, warmup, flush, main=False, min_s=0.0):
+    """Mean CUDA-event time of `steps` calls of fn (L2 flushed before each)
+    after `warmup` calls; with min_s > 0 the timed calls go on until they
+    span at least min_s seconds, so that the clock sampler (10 ms period)
+    sees the timed region.  main: record the window and step count in
+    _MAIN."""
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize()
     times = []
-    for _ in range(steps):
+    w0 = time.time()
+    while len(times) < steps or time.time() - w0 < min_s:
         if flush is not None:
             flush.fill_(1.0)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -728,6 +744,9 @@ def _timed_events(torch, fn, steps, warmup, flush):
         e1.record()
         e1.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
+    if main:
+        _MAIN["window"] = (w0, time.time())
+        _MAIN["steps"] = len(times)
     return statistics.mean(times)
 
 
@@ -797,7 +816,8 @@ def wl_krige(args, torch, gg, flush):
     dm, dv, dc = (torch.from_numpy(np.ascontiguousarray(x)).to(dev)
                   for x in (mat, vecs, cond))
     step = lambda: gg.calc_field_krige_and_variance(dm, dv, dc)
-    t = _timed_events(torch, step, args.steps, args.warmup, flush)
+    t = _timed_events(torch, step, args.steps, args.warmup, flush, main=True,
+                      min_s=args.min_timed_s)
     f, e = step()
     # the field alone: V^T (M^T c), one pass over V (HBM-bound)
     t_field = _timed_events(torch, lambda: gg.calc_field_krige(dm, dv, dc),
@@ -870,7 +890,8 @@ def wl_vario(args, torch, gg, flush):
         _native.call("gst_vario_unstructured", 2, n, 1, p(dfd), nb, p(de), p(dp),
                      ord("m"), ord("e"), p(vario), p(counts), stream)
 
-    t = _timed_events(torch, step, args.steps, args.warmup, flush)
+    t = _timed_events(torch, step, args.steps, args.warmup, flush, main=True,
+                      min_s=args.min_timed_s)
     pairs = n * (n - 1) / 2
     # directional: the two axes, tolerance pi/8, bandwidth 20
     dirs = torch.tensor([[1.0, 0.0], [0.0, 1.0]], dtype=torch.float64, device=dev)
@@ -948,7 +969,8 @@ def wl_points(args, torch, gg, flush):
     f64 = lambda: gg.summate(*t)
     mixed = lambda: gg.summate(*t, precision="mixed")
     t64 = _timed_events(torch, f64, args.steps, args.warmup, flush)
-    tmx = _timed_events(torch, mixed, args.steps, args.warmup, flush)
+    tmx = _timed_events(torch, mixed, args.steps, args.warmup, flush, main=True,
+                        min_s=args.min_timed_s)
     t0 = time.perf_counter()
     ref = oracle.c_summate(gen.cov_samples, gen.z_1, gen.z_2, pos)
     t_cpu = time.perf_counter() - t0
@@ -982,7 +1004,7 @@ def wl_points(args, torch, gg, flush):
                           "sin/cos; the exact turn reduction issues ~20 FP32 "
                           "operations per mode*point, and ncu measures the FMA "
                           "pipe 64.8 % active (profiles: pointwise summary)"},
-        gpu_launches=2 * args.steps)
+        gpu_launches=2 * _MAIN["steps"])
 
 
 def make_ensemble(n_items=512, seed=20170519):
@@ -1016,7 +1038,8 @@ def wl_ensemble(args, torch, gg, flush):
     bs.load([g.cov_samples for g in gens], [g.z_1 for g in gens],
             [g.z_2 for g in gens], pos, scales)
     tune = bs.tune()
-    t_batch = _timed_events(torch, bs.run, args.steps, args.warmup, flush)
+    t_batch = _timed_events(torch, bs.run, args.steps, args.warmup, flush, main=True,
+                            min_s=args.min_timed_s)
     batched = [f.astype(np.float64) for f in bs.split()]
     # modes drawn on the device (one Philox stream per realization seed) vs
     # the host mirror's per-realization reset_seed loop (the reference's way)
@@ -1129,7 +1152,7 @@ def wl_ensemble(args, torch, gg, flush):
                                        + sum(c.nbytes for c in cov_l) * 2),
              "d2h_bytes_per_step": int(sum(r.nbytes for r in res))},
         cpu_baseline=cpu,
-        gpu_launches=2 * args.steps)
+        gpu_launches=2 * _MAIN["steps"])
 
 
 def wl_incompr(args, torch, gg, flush):
@@ -1155,7 +1178,8 @@ def wl_incompr(args, torch, gg, flush):
     tensor = lambda: _native.call("gst_summate_incompr_grid_tc", 3, nm, lens,
                                   p(axes), p(d[0]), p(d[0]), p(d[1]), p(d[2]),
                                   p(out_tc), _native.GST_OUT_F32, scale, stream)
-    ttc = _timed_events(torch, tensor, args.steps, args.warmup, flush)
+    ttc = _timed_events(torch, tensor, args.steps, args.warmup, flush, main=True,
+                        min_s=args.min_timed_s)
     tmx = _timed_events(torch, mixed, args.steps, args.warmup, flush)
     slab = 12
     lens64 = (ctypes.c_int64 * 4)(slab, n, n, 1)
@@ -1223,7 +1247,7 @@ def wl_incompr(args, torch, gg, flush):
         divergence={"fd_rms_over_grad_rms": float(div.std() / grad_scale),
                     "note": "central differences, h=1; O(h^2) truncation"},
         cpu_baseline=cpu,
-        gpu_launches=2 * args.steps)
+        gpu_launches=2 * _MAIN["steps"])
 
 
 def wl_adjoint(args, torch, gg, flush):
@@ -1271,7 +1295,8 @@ def wl_adjoint(args, torch, gg, flush):
             t.grad = None
         loss_of(fwd(prec)).backward()
 
-    t_f = _timed_events(torch, step_fwd, args.steps, args.warmup, flush)
+    t_f = _timed_events(torch, step_fwd, args.steps, args.warmup, flush, main=True,
+                        min_s=args.min_timed_s)
     t_fb = _timed_events(torch, step_fwd_bwd, args.steps, args.warmup, flush)
     # the adjoint over every point (the cotangent is zero off the 10 000
     # observations, which the default backward leaves out)
@@ -1333,19 +1358,21 @@ _LINE_ONLY = ("metric", "n_gpus", "steps", "warmup", "higher_is_better",
 
 def other_configs(args, torch, gg, flush):
     """Bounded runs of the other four configurations for the headline line:
-    5 timed steps after 3 warm-up steps each, every one with its error
-    against the oracle and the clocks sampled over its own run."""
+    at least 5 timed steps spanning at least --min-timed-s seconds after 3
+    warm-up steps each, every one with its error against the oracle and the
+    clocks sampled inside the timed region of its `value`."""
     sub = argparse.Namespace(**vars(args))
     sub.steps, sub.warmup, sub.size = 5, 3, "full"
     out = {}
     for fn in (wl_points, wl_ensemble, wl_incompr, wl_adjoint):
         ck = Clocks(torch.cuda.current_device())
         ck.start()
+        _MAIN["window"], _MAIN["steps"] = None, 0
         line = fn(sub, torch, gg, flush)
-        clk = ck.stop()
+        clk = ck.stop(window=_MAIN["window"])
         keep = {k: v for k, v in line.items() if k not in _LINE_ONLY}
         keep["clocks"] = clk
-        keep["steps"], keep["warmup"] = sub.steps, sub.warmup
+        keep["steps"], keep["warmup"] = _MAIN["steps"], sub.warmup
         out[line["config"]["workload"]] = keep
     return out
 
@@ -1365,7 +1392,9 @@ def run_workload(args):
     clocks = Clocks(0)
     clocks.start()
     line = fn(args, torch, gg, flush)
-    line["clocks"] = clocks.stop()
+    line["clocks"] = clocks.stop(window=_MAIN["window"])
+    if _MAIN["steps"]:
+        line["steps"] = _MAIN["steps"]
     print(json.dumps(line), flush=True)
 
 
