@@ -1254,7 +1254,9 @@ def wl_adjoint(args, torch, gg, flush):
     """3-D Gaussian, 4000 modes (reference RNG, anisotropic and rotated),
     128^3 grid + 50 000 points in [0, 128]^3; loss = mean squared misfit at
     10 000 random observation points against a field from another seed;
-    gradients w.r.t. z_1, z_2, len_scale, anisotropy and rotation angles."""
+    gradients w.r.t. z_1, z_2, len_scale, anisotropy and rotation angles.
+    The grid is passed as its axes (structured forward), the points as
+    coordinates."""
     from gstools_gb300.grad import isometrize_matrix, randmeth_field
 
     data = np.load(os.path.join(ROOT, "tests", "golden", "workloads.npz"))
@@ -1266,7 +1268,8 @@ def wl_adjoint(args, torch, gg, flush):
     g = np.arange(128.0)
     grid = np.array(np.meshgrid(g, g, g, indexing="ij")).reshape(3, -1)
     pts = np.concatenate([grid, rng.uniform(0.0, 128.0, (3, 50_000))], axis=1)
-    x = torch.tensor(pts, device=dev)
+    x = torch.tensor(pts[:, g.size ** 3:], device=dev)   # the 50 000 points
+    axes = [torch.tensor(g, device=dev)] * 3
     obs = torch.tensor(rng.choice(pts.shape[1], 10_000, replace=False), device=dev)
     other = gg.RandMeth(gg.Gaussian(dim=3, var=1.0, len_scale=16.0), mode_no=4000,
                         seed=4242, sampling="analytic")
@@ -1281,7 +1284,10 @@ def wl_adjoint(args, torch, gg, flush):
                                      device=dev, requires_grad=True)}
 
     def fwd(prec):
-        return randmeth_field(cov_ref, 16.0, z1, z2, x, precision=prec, **params)
+        # the 128^3 grid (tensor-core contraction forward in mixed precision)
+        # followed by the 50 000 points
+        return randmeth_field(cov_ref, 16.0, z1, z2, x, axes=axes, precision=prec,
+                              **params)
 
     def loss_of(u):
         return torch.mean((u[obs] - target) ** 2)
@@ -1339,8 +1345,13 @@ def wl_adjoint(args, torch, gg, flush):
                       skip=args.no_cpu_baseline)
     return _line(
         args, "gau3d_adjoint_grid128_pts50k_modes4000", work / t_f / 1e9, t_f,
-        "fp32 + exact turn reduction",
+        "f16x3 (grid) + fp32 with exact turn reduction (points)",
         {"points": int(pts.shape[1]), "modes": 4000, "observations": 10_000},
+        notes={"path": "randmeth_field(pos=50k points, axes=128^3 grid): the "
+                       "grid forward through the tensor-core contraction "
+                       "(SummateGridFunction), the points through the mixed "
+                       "pointwise kernel; the backward runs the adjoint "
+                       "kernels at the points with a nonzero cotangent"},
         fwd_ms=t_f * 1e3, fwd_bwd_ms=t_fb * 1e3, fwd_bwd_over_fwd=t_fb / t_f,
         fwd_bwd_all_points={"ms": t_fb_dense * 1e3, "over_fwd": t_fb_dense / t_f,
                             "note": "adjoint kernels over all 2.15 M points, "

@@ -273,10 +273,76 @@ int run_vjp_modes(int prec, int dim, int64_t n_modes, int64_t n_pts,
     return GST_OK;
 }
 
+struct GatherGeom {
+    int dim;
+    int64_t n[3];     // grid axis lengths
+    int64_t off[3];   // offsets of the axes in the concatenated array
+    int64_t n_grid, n_extra;
+};
+
+// Coordinates and cotangent of point idx[t] (a grid point in "ij" order, or
+// point idx - n_grid of the extra points).
+__global__ void gather_points_kernel(GatherGeom gg, const double *__restrict__ axes,
+                                     const double *__restrict__ x_extra, int64_t n_idx,
+                                     const int64_t *__restrict__ idx,
+                                     const double *__restrict__ g, double *xs,
+                                     double *gs) {
+    const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (t >= n_idx) return;
+    const int64_t i = idx[t];
+    const bool ok = i >= 0 && i < gg.n_grid + gg.n_extra;
+    if (ok && i < gg.n_grid) {
+        int64_t rest = i;
+        for (int d = gg.dim - 1; d >= 0; --d) {
+            const int64_t n = d == 0 ? gg.n[0] : (d == 1 ? gg.n[1] : gg.n[2]);
+            const int64_t o = d == 0 ? gg.off[0] : (d == 1 ? gg.off[1] : gg.off[2]);
+            xs[d * n_idx + t] = axes[o + rest % n];
+            rest /= n;
+        }
+    } else {
+        for (int d = 0; d < gg.dim; ++d)
+            xs[d * n_idx + t] = ok ? x_extra[d * gg.n_extra + (i - gg.n_grid)] : 0.0;
+    }
+    gs[t] = ok ? g[i] : 0.0;
+}
+
 }  // namespace
 }  // namespace gst
 
 extern "C" {
+
+int gst_gather_points(int dim, const int64_t *axis_len, const double *axes,
+                      int64_t n_extra, const double *x_extra, int64_t n_idx,
+                      const int64_t *idx, const double *g, double *xs,
+                      double *gs, void *stream) {
+    using namespace gst;
+    if (dim < 1 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
+    if (axis_len == nullptr || n_extra < 0 || n_idx < 0) return GST_ERR_INVALID_ARGUMENT;
+    if (n_idx == 0) return GST_OK;
+    GatherGeom geo{};
+    geo.dim = dim;
+    geo.n_grid = 1;
+    int64_t off = 0;
+    for (int d = 0; d < dim; ++d) {
+        if (axis_len[d] < 0) return GST_ERR_INVALID_ARGUMENT;
+        geo.n[d] = axis_len[d];
+        geo.off[d] = off;
+        off += axis_len[d];
+        geo.n_grid *= axis_len[d];
+    }
+    geo.n_extra = n_extra;
+    if (idx == nullptr || g == nullptr || xs == nullptr || gs == nullptr ||
+        (geo.n_grid > 0 && axes == nullptr) || (n_extra > 0 && x_extra == nullptr))
+        return GST_ERR_INVALID_ARGUMENT;
+    if (current_device() < 0) return GST_ERR_NO_DEVICE;
+    const int64_t blocks = ceil_div(n_idx, 256);
+    if (blocks > 0x7fffffffLL) return GST_ERR_TOO_LARGE;
+    gather_points_kernel<<<static_cast<unsigned>(blocks), 256, 0,
+                           static_cast<cudaStream_t>(stream)>>>(geo, axes, x_extra, n_idx,
+                                                                idx, g, xs, gs);
+    GST_TRY_CUDA(cudaGetLastError());
+    return GST_OK;
+}
 
 int gst_summate_vjp_modes_f64(int dim, int64_t n_modes, int64_t n_pts,
                               const double *cov_samples, const double *z_1,

@@ -27,8 +27,9 @@ import torch
 from . import _native, config
 from .summator import _p, _stream, device
 
-__all__ = ["SummateFunction", "summate_torch", "isometrize_matrix",
-           "randmeth_field", "SPARSE_COTANGENT"]
+__all__ = ["SummateFunction", "SummateGridFunction", "summate_torch",
+           "summate_grid_torch", "isometrize_matrix", "randmeth_field",
+           "SPARSE_COTANGENT"]
 
 # Run the adjoint kernels on the points with a nonzero cotangent only, when
 # at most a quarter of the points have one (read at every backward).  The
@@ -39,6 +40,54 @@ SPARSE_COTANGENT = True
 
 def _dev_f64(t, dev):
     return t.detach().to(device=dev, dtype=torch.float64).contiguous()
+
+
+def _cotangent_support(g, n_pts):
+    """Indices of the points with a nonzero cotangent when at most a quarter
+    of the points have one (one device sync), else None (all points)."""
+    if not SPARSE_COTANGENT or n_pts == 0:
+        return None
+    idx = torch.nonzero(g).reshape(-1)
+    return idx if 4 * idx.numel() <= n_pts else None
+
+
+def _adjoint(ctx, g, cov, z1, z2, n_pts, gather, need_pos):
+    """The mode (and position) gradients of ``u = summate(cov, z1, z2, x)``
+    for the cotangent g; ``gather(idx)`` gives the coordinates and the
+    cotangents of the points idx, or of all points for idx None.  Points
+    whose cotangent is exactly zero add nothing to the mode gradients and
+    get a zero position gradient; when at most a quarter of the points carry
+    one (a loss on a subset of the field) the adjoint kernels run on those
+    points only."""
+    dev = cov.device
+    dim, n_modes = cov.shape
+    stream = _stream(dev)
+    need_cov, need_z1, need_z2 = ctx.needs_input_grad[:3]
+    d_cov = d_z1 = d_z2 = d_pos = None
+    idx = _cotangent_support(g, n_pts)
+    xs, gs = gather(idx)
+    n_sel = xs.shape[1]
+    if need_cov or need_z1 or need_z2:
+        gz1 = torch.empty(n_modes, dtype=torch.float64, device=dev)
+        gz2 = torch.empty(n_modes, dtype=torch.float64, device=dev)
+        gk = torch.empty((dim, n_modes), dtype=torch.float64, device=dev)
+        _native.call(f"gst_summate_vjp_modes_{ctx.prec}", dim, n_modes,
+                     n_sel, _p(cov), _p(z1), _p(z2), _p(xs), _p(gs),
+                     _p(gz1), _p(gz2), _p(gk), stream)
+        d_cov = gk.to(ctx.in_devices[0]) if need_cov else None
+        d_z1 = gz1.to(ctx.in_devices[1]) if need_z1 else None
+        d_z2 = gz2.to(ctx.in_devices[2]) if need_z2 else None
+    if need_pos:
+        v = torch.empty((dim, n_sel), dtype=torch.float64, device=dev)
+        _native.call(f"gst_summate_vjp_pos_{ctx.prec}", dim, n_modes,
+                     n_sel, _p(cov), _p(z1), _p(z2), _p(xs), _p(v), stream)
+        if idx is None:
+            d_pos = v * g
+        else:
+            d_pos = torch.zeros((dim, n_pts), dtype=torch.float64, device=dev)
+            d_pos.index_copy_(1, idx, v * gs)
+        d_pos = d_pos.to(ctx.in_devices[3])
+    return d_cov, d_z1, d_z2, d_pos
 
 
 class SummateFunction(torch.autograd.Function):
@@ -67,51 +116,113 @@ class SummateFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_out):
         cov, z1, z2, x = ctx.saved_tensors
-        dev = cov.device
-        dim, n_modes = cov.shape
-        n_pts = x.shape[1]
-        g = _dev_f64(grad_out, dev).reshape(-1)
-        stream = _stream(dev)
-        need_cov, need_z1, need_z2, need_pos = ctx.needs_input_grad[:4]
-        d_cov = d_z1 = d_z2 = d_pos = None
-        # Points whose cotangent is exactly zero add nothing to the mode
-        # gradients and get a zero position gradient; when at most a quarter
-        # of the points carry one (a loss on a subset of the field) the
-        # adjoint kernels run on those points only.
-        idx = None
-        if SPARSE_COTANGENT and n_pts > 0:
-            nnz = int(torch.count_nonzero(g))
-            if 4 * nnz <= n_pts:
-                idx = torch.nonzero(g).reshape(-1)
-        xs, gs = (x, g) if idx is None else (x.index_select(1, idx).contiguous(),
-                                             g.index_select(0, idx).contiguous())
-        n_sel = xs.shape[1]
-        if need_cov or need_z1 or need_z2:
-            gz1 = torch.empty(n_modes, dtype=torch.float64, device=dev)
-            gz2 = torch.empty(n_modes, dtype=torch.float64, device=dev)
-            gk = torch.empty((dim, n_modes), dtype=torch.float64, device=dev)
-            _native.call(f"gst_summate_vjp_modes_{ctx.prec}", dim, n_modes,
-                         n_sel, _p(cov), _p(z1), _p(z2), _p(xs), _p(gs),
-                         _p(gz1), _p(gz2), _p(gk), stream)
-            d_cov = gk.to(ctx.in_devices[0]) if need_cov else None
-            d_z1 = gz1.to(ctx.in_devices[1]) if need_z1 else None
-            d_z2 = gz2.to(ctx.in_devices[2]) if need_z2 else None
-        if need_pos:
-            v = torch.empty((dim, n_sel), dtype=torch.float64, device=dev)
-            _native.call(f"gst_summate_vjp_pos_{ctx.prec}", dim, n_modes,
-                         n_sel, _p(cov), _p(z1), _p(z2), _p(xs), _p(v), stream)
+        g = _dev_f64(grad_out, cov.device).reshape(-1)
+
+        def gather(idx):
             if idx is None:
-                d_pos = v * g
-            else:
-                d_pos = torch.zeros((dim, n_pts), dtype=torch.float64, device=dev)
-                d_pos.index_copy_(1, idx, v * gs)
-            d_pos = d_pos.to(ctx.in_devices[3])
-        return d_cov, d_z1, d_z2, d_pos, None
+                return x, g
+            return (x.index_select(1, idx).contiguous(),
+                    g.index_select(0, idx).contiguous())
+
+        grads = _adjoint(ctx, g, cov, z1, z2, x.shape[1], gather,
+                         ctx.needs_input_grad[3])
+        return (*grads, None)
+
+
+class SummateGridFunction(torch.autograd.Function):
+    """``u = summate`` on the structured grid spanned by ``axes`` ("ij"
+    order, flattened), followed by the points ``pos`` when given,
+    differentiable in the modes and in ``pos``.
+
+    Mixed precision runs the grid forward through the separable tensor-core
+    contraction, FP64 through the FP64 grid kernel; the points run the
+    pointwise kernels.  The backward is one adjoint call, as in
+    :class:`SummateFunction`, on the grid points and points with a nonzero
+    cotangent (grid coordinates gathered from the axes).  The axes get no
+    gradient."""
+
+    @staticmethod
+    def forward(ctx, cov_samples, z_1, z_2, pos, axes, precision):
+        prec = config.check_precision(precision)
+        dev = device()
+        cov = _dev_f64(cov_samples, dev)
+        z1 = _dev_f64(z_1, dev).reshape(-1)
+        z2 = _dev_f64(z_2, dev).reshape(-1)
+        dim, n_modes = cov.shape
+        ax = [_dev_f64(torch.as_tensor(a), dev).reshape(-1) for a in axes]
+        if len(ax) != dim:
+            raise ValueError("one axis per dimension of cov_samples")
+        from .summator import summate_grid
+
+        if prec == "mixed" and dim in (2, 3):
+            grid = summate_grid(cov, z1, z2, ax, precision="mixed", method="tensor",
+                                out_dtype="float64").reshape(-1)
+        else:
+            grid = summate_grid(cov, z1, z2, ax, precision=prec,
+                                method="pointwise").reshape(-1)
+        x = (torch.empty((dim, 0), dtype=torch.float64, device=dev) if pos is None
+             else _dev_f64(pos, dev).reshape(dim, -1))
+        out = grid
+        if x.shape[1] > 0:
+            out = torch.empty(grid.numel() + x.shape[1], dtype=torch.float64,
+                              device=dev)
+            out[:grid.numel()] = grid
+            name = "gst_summate_f64" if prec == "f64" else "gst_summate_mixed"
+            args = [dim, n_modes, x.shape[1], _p(cov), _p(z1), _p(z2), _p(x),
+                    _p(out[grid.numel():])]
+            if prec == "mixed":
+                args.append(_native.GST_OUT_F64)
+            _native.call(name, *args, _stream(dev))
+        ctx.save_for_backward(cov, z1, z2, x, *ax)
+        ctx.prec = prec
+        ctx.in_devices = [t.device for t in (cov_samples, z_1, z_2)] + [
+            dev if pos is None else pos.device]
+        ctx.shape = tuple(a.numel() for a in ax)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        cov, z1, z2, x, *ax = ctx.saved_tensors
+        g = _dev_f64(grad_out, cov.device).reshape(-1)
+        shape = ctx.shape
+        n_grid = 1
+        for n in shape:
+            n_grid *= n
+
+        def gather(idx):
+            if idx is None:
+                mesh = torch.meshgrid(*ax, indexing="ij")
+                grid = torch.stack([m.reshape(-1) for m in mesh])
+                return torch.cat([grid, x], 1).contiguous(), g
+            # one kernel: grid points unravelled from the axes, extra points
+            # copied, cotangents picked
+            n = idx.numel()
+            xs = torch.empty((len(ax), n), dtype=torch.float64, device=g.device)
+            gs = torch.empty(n, dtype=torch.float64, device=g.device)
+            lens = (ctypes.c_int64 * 3)(*(list(shape) + [1] * (3 - len(shape))))
+            flat = torch.cat(ax)
+            _native.call("gst_gather_points", len(ax), lens, _p(flat), x.shape[1],
+                         _p(x), n, _p(idx), _p(g), _p(xs), _p(gs), _stream(g.device))
+            return xs, gs
+
+        need_pos = ctx.needs_input_grad[3] and x.shape[1] > 0
+        d_cov, d_z1, d_z2, d_pos = _adjoint(ctx, g, cov, z1, z2, n_grid + x.shape[1],
+                                            gather, need_pos)
+        if d_pos is not None:
+            d_pos = d_pos[:, n_grid:]
+        return d_cov, d_z1, d_z2, d_pos, None, None
 
 
 def summate_torch(cov_samples, z_1, z_2, pos, precision=None):
     """Differentiable ``summate`` on torch tensors (float64 result)."""
     return SummateFunction.apply(cov_samples, z_1, z_2, pos, precision)
+
+
+def summate_grid_torch(cov_samples, z_1, z_2, axes, precision=None):
+    """Differentiable ``summate`` on the structured grid spanned by ``axes``
+    (float64, flattened in "ij" order; no gradient w.r.t. the axes)."""
+    return SummateGridFunction.apply(cov_samples, z_1, z_2, None, tuple(axes),
+                                     precision)
 
 
 def _givens(dim, plane, angle):
@@ -150,14 +261,104 @@ def isometrize_matrix(dim, angles, anis):
     return stretch @ rot
 
 
-def randmeth_field(cov_ref, len_scale_ref, z_1, z_2, pos, *, var, len_scale,
-                   anis, angles, precision=None):
-    """Field at physical positions ``pos`` (dim, n), differentiable in every
-    tensor argument (``var``, ``len_scale``, ``anis``, ``angles``, ``z_1``,
-    ``z_2``, ``pos``).  ``cov_ref`` are the model's wave vectors drawn at
-    ``len_scale_ref``."""
+def _givens_np(dim, plane, theta):
+    """Givens rotation by theta in `plane` and its derivative in theta."""
+    import numpy as np
+
+    p, q = plane
+    c, s = np.cos(theta), np.sin(theta)
+    g = np.eye(dim)
+    dg = np.zeros((dim, dim))
+    g[p, p] = g[q, q] = c
+    g[p, q], g[q, p] = -s, s
+    dg[p, p] = dg[q, q] = -s
+    dg[p, q], dg[q, p] = -c, c
+    return g, dg
+
+
+class _ModeMap(torch.autograd.Function):
+    """``M(angles, anis)^T * (len_scale_ref / len_scale)`` on the host from
+    the packed parameters [len_scale, anis..., angles...] (a CPU float64
+    tensor), with its analytic derivative: M = diag(1, 1/anis) R_0 R_1 ...,
+    R_i the Givens rotation of plane i by (-1)^i (-angles_i) -- the
+    construction of :func:`isometrize_matrix` -- in a few numpy operations
+    instead of a few dozen autograd nodes."""
+
+    @staticmethod
+    def forward(ctx, packed, dim, len_scale_ref):
+        import numpy as np
+
+        v = packed.detach().numpy()
+        n_anis = dim - 1
+        ls, anis, angles = v[0], v[1:1 + n_anis], v[1 + n_anis:]
+        planes = [(i, j) for j in range(1, dim) for i in range(j)]
+        gs = [_givens_np(dim, pl, (-1) ** i * (-angles[i]))
+              for i, pl in enumerate(planes)]
+        rot = np.eye(dim)
+        for g, _ in gs:
+            rot = rot @ g
+        stretch = np.diag(np.concatenate([[1.0], 1.0 / anis]))
+        m = stretch @ rot
+        r = len_scale_ref / ls
+        ctx.parts = (dim, ls, anis, r, gs, rot, stretch, m)
+        return torch.from_numpy((m.T * r).copy())
+
+    @staticmethod
+    def backward(ctx, grad_mt):
+        import numpy as np
+
+        dim, ls, anis, r, gs, rot, stretch, m = ctx.parts
+        gmt = grad_mt.detach().to("cpu", torch.float64).numpy()
+        d_ls = -np.sum(gmt * m.T) * r / ls
+        gm = r * gmt.T                      # dL/dM
+        gs_ = gm @ rot.T                    # dL/dstretch
+        grot = stretch.T @ gm               # dL/drot
+        d_anis = np.array([gs_[j + 1, j + 1] * (-1.0 / anis[j] ** 2)
+                           for j in range(dim - 1)])
+        d_angles = []
+        for i in range(len(gs)):
+            left = np.eye(dim)
+            for g, _ in gs[:i]:
+                left = left @ g
+            right = np.eye(dim)
+            for g, _ in gs[i + 1:]:
+                right = right @ g
+            dtheta = np.sum((left.T @ grot @ right.T) * gs[i][1])
+            d_angles.append(dtheta * -((-1) ** i))
+        grad = np.concatenate([[d_ls], d_anis, np.array(d_angles)])
+        return torch.from_numpy(grad), None, None
+
+
+def randmeth_field(cov_ref, len_scale_ref, z_1, z_2, pos=None, *, var, len_scale,
+                   anis, angles, precision=None, axes=None):
+    """Field at physical positions ``pos`` (dim, n) and/or on the
+    structured grid spanned by ``axes`` (flattened, "ij" order; with both,
+    the grid's values come first), differentiable in every tensor argument
+    (``var``, ``len_scale``, ``anis``, ``angles``, ``z_1``, ``z_2`` and
+    ``pos``; not the axes).  ``cov_ref`` are the model's wave vectors drawn
+    at ``len_scale_ref``.  A mixed-precision grid runs the tensor-core
+    contraction forward."""
+    if pos is None and axes is None:
+        raise ValueError("give pos, axes or both")
     dim, n_modes = cov_ref.shape
-    m = isometrize_matrix(dim, angles, anis).to(cov_ref.device)
-    k = m.T @ (cov_ref * (len_scale_ref / len_scale))
-    return torch.sqrt(var / n_modes) * summate_torch(k, z_1, z_2, pos,
-                                                     precision)
+    # The dim x dim map M^T (len_scale_ref / len_scale) is built on the host
+    # from one host copy of the small parameters (differentiable: autograd
+    # copies their gradients back), so its few dozen scalar operations and
+    # their backward are no device launches; one dim x dim @ dim x N product
+    # runs on the device.
+    small = [torch.as_tensor(t, dtype=torch.float64).reshape(-1)
+             for t in (len_scale, anis, angles)]
+    devs = {t.device for t in small}
+    if len(devs) == 1:
+        host = torch.cat(small).to("cpu")
+    else:
+        host = torch.cat([t.to("cpu") for t in small])
+    if small[1].numel() != dim - 1 or small[2].numel() != dim * (dim - 1) // 2:
+        raise ValueError("need dim - 1 anisotropy ratios and dim (dim - 1) / 2 angles")
+    mt = _ModeMap.apply(host, dim, float(len_scale_ref))
+    k = mt.to(device=cov_ref.device, dtype=cov_ref.dtype) @ cov_ref
+    if axes is not None:
+        u = SummateGridFunction.apply(k, z_1, z_2, pos, tuple(axes), precision)
+    else:
+        u = summate_torch(k, z_1, z_2, pos, precision)
+    return torch.sqrt(var / n_modes) * u

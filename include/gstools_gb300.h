@@ -272,6 +272,16 @@ int gst_summate_vjp_pos_mixed(int dim, int64_t n_modes, int64_t n_pts,
                               const double *cov_samples, const double *z_1,
                               const double *z_2, const double *pos, double *out,
                               void *stream);
+/* The points of a structured grid (axes concatenated, "ij" order, axis_len
+ * with dim entries) followed by n_extra points x_extra (dim, n_extra) that
+ * the n_idx indices idx (device int64) select: xs (dim, n_idx) their
+ * coordinates and gs (n_idx,) = g[idx] their cotangents -- the inputs of
+ * gst_summate_vjp_* for the points of a field with a nonzero cotangent.
+ * An index outside [0, grid points + n_extra) gives zeros. */
+int gst_gather_points(int dim, const int64_t *axis_len, const double *axes,
+                      int64_t n_extra, const double *x_extra, int64_t n_idx,
+                      const int64_t *idx, const double *g, double *xs,
+                      double *gs, void *stream);
 
 /* ----------------------------------------------------------------------- */
 /* Batched ensembles: many realizations with their own modes and point sets. */

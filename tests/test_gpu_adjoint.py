@@ -163,3 +163,105 @@ def test_sparse_cotangent_matches_all_points(cuda_lib, precision, tol):
     mask = torch.ones(40_000, dtype=torch.bool, device="cuda")
     mask[obs] = False
     assert torch.all(results[True][3][:, mask] == 0)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("sparse", [True, False])
+def test_grid_function_matches_point_function(cuda_lib, dim, sparse):
+    """The structured-grid form (tensor-core forward in mixed precision, the
+    FP64 grid kernel in FP64; adjoint on the grid points gathered from the
+    axes) against the point form on the meshgrid of the same axes: fields
+    and mode gradients of a loss on a subset (sparse cotangent) or on every
+    point (dense)."""
+    from gstools_gb300 import grad
+    from gstools_gb300.grad import summate_grid_torch
+
+    cov, z1, z2, _, _ = leaves(30 + dim, dim, 600, 10)
+    shape = (40, 36, 20)[:dim]
+    axes = [torch.linspace(-30.0, 50.0, n, dtype=torch.float64, device="cuda")
+            for n in shape]
+    mesh = torch.stack([m.reshape(-1) for m in
+                        torch.meshgrid(*axes, indexing="ij")]).contiguous()
+    n = mesh.shape[1]
+    obs = torch.arange(0, n, 37, device="cuda") if sparse else torch.arange(
+        n, device="cuda")
+    target = torch.randn(obs.numel(), dtype=torch.float64, device="cuda")
+    tol = {"f64": (1e-12, 1e-10), "mixed": (2e-5, 1e-4)}
+    for prec in ("f64", "mixed"):
+        res = {}
+        for form in ("grid", "points"):
+            for t in (cov, z1, z2):
+                t.grad = None
+            u = (summate_grid_torch(cov, z1, z2, axes, prec) if form == "grid"
+                 else summate_torch(cov, z1, z2, mesh, prec))
+            torch.mean((u[obs] - target) ** 2).backward()
+            res[form] = [u.detach()] + [t.grad.clone() for t in (cov, z1, z2)]
+        assert grad.SPARSE_COTANGENT
+        ftol, gtol = tol[prec]
+        assert rel(res["grid"][0], res["points"][0]) <= ftol, (prec, "field")
+        for name, a, b in zip(("cov", "z1", "z2"), res["grid"][1:],
+                              res["points"][1:]):
+            assert rel(a, b) <= gtol, (prec, name, rel(a, b))
+
+
+def test_randmeth_field_grid_and_points(cuda_lib, workloads):
+    """randmeth_field on a grid plus scattered points (the grid's values
+    first) equals the point form on the meshgrid followed by the points, and
+    so do the gradients of the points and the model parameters (FP64)."""
+    c = workloads.case("gau3d_grad")
+    dev = "cuda"
+    cov_ref = torch.tensor(c["cov"][:, :300], device=dev)
+    z1 = torch.tensor(c["z1"][:300], device=dev)
+    z2 = torch.tensor(c["z2"][:300], device=dev)
+    axes = [torch.arange(float(n), dtype=torch.float64, device=dev) * 2.0
+            for n in (12, 10, 8)]
+    mesh = torch.stack([m.reshape(-1) for m in
+                        torch.meshgrid(*axes, indexing="ij")])
+    pts = (torch.rand((3, 500), dtype=torch.float64, device=dev) * 24.0
+           ).requires_grad_(True)
+    p0 = {"len_scale": 16.0, "anis": [0.8, 0.6], "angles": [0.3, 0.2, 0.1],
+          "var": 1.0}
+    res = {}
+    for form in ("grid", "points"):
+        pts.grad = None
+        params = {k: torch.tensor(v, dtype=torch.float64, device=dev,
+                                  requires_grad=True) for k, v in p0.items()}
+        if form == "grid":
+            u = randmeth_field(cov_ref, 16.0, z1, z2, pts, axes=axes,
+                               precision="f64", **params)
+        else:
+            u = randmeth_field(cov_ref, 16.0, z1, z2, torch.cat([mesh, pts], 1),
+                               precision="f64", **params)
+        torch.sum(u[::7] ** 2).backward()
+        res[form] = [u.detach(), pts.grad.clone()] + [
+            params[k].grad.clone() for k in ("len_scale", "anis", "angles", "var")]
+    for a, b in zip(res["grid"], res["points"]):
+        assert rel(a, b) <= 1e-10
+
+
+def test_gather_points_kernel(cuda_lib):
+    """gst_gather_points: grid points unravelled from the axes ("ij"), extra
+    points copied, cotangents picked; an out-of-range index gives zeros."""
+    import ctypes
+
+    from gstools_gb300 import _native
+    from gstools_gb300.summator import _p, _stream
+
+    dev = torch.device("cuda")
+    ax = [torch.linspace(0.0, 1.0, n, dtype=torch.float64, device=dev) + 10.0 * d
+          for d, n in enumerate((5, 4, 3))]
+    extra = torch.randn(3, 7, dtype=torch.float64, device=dev)
+    mesh = torch.stack([m.reshape(-1) for m in torch.meshgrid(*ax, indexing="ij")])
+    allx = torch.cat([mesh, extra], 1)
+    g = torch.randn(allx.shape[1], dtype=torch.float64, device=dev)
+    idx = torch.tensor([0, 7, 59, 60, 66, 3, 67, -1], dtype=torch.int64, device=dev)
+    xs = torch.empty(3, idx.numel(), dtype=torch.float64, device=dev)
+    gs = torch.empty(idx.numel(), dtype=torch.float64, device=dev)
+    lens = (ctypes.c_int64 * 3)(5, 4, 3)
+    _native.call("gst_gather_points", 3, lens, _p(torch.cat(ax)), 7, _p(extra),
+                 idx.numel(), _p(idx), _p(g), _p(xs), _p(gs), _stream(dev))
+    torch.cuda.synchronize()
+    good = idx[:6]
+    assert torch.equal(xs[:, :6], allx[:, good])
+    assert torch.equal(gs[:6], g[good])
+    assert torch.all(xs[:, 6:] == 0) and torch.all(gs[6:] == 0)
