@@ -688,10 +688,13 @@ int gst_summate_mixed(int dim, int64_t n_modes, int64_t n_pts,
     if (!gst::valid_out_type(out_type)) return GST_ERR_INVALID_ARGUMENT;
     // Large sums take the sorted amplitude-phase path (gst_batched.cu): its
     // prologue (mode and point sorts, ~0.15 ms at 1e5 points) pays off from
-    // about 2e8 mode-points on; smaller ones, and mode sets beyond what its
-    // one-CTA mode sort handles quickly, run the pointwise kernel here.
+    // about 4e8 mode-points over 2e5 points on; smaller ones, and mode sets
+    // beyond what its one-CTA mode sort handles quickly, run the pointwise
+    // kernel here.
+    const double work = static_cast<double>(n_modes) * static_cast<double>(n_pts);
     if (n_modes > 0 && n_pts > 0 && n_modes <= gst::kSortedMaxModes &&
-        static_cast<double>(n_modes) * static_cast<double>(n_pts) >= gst::kSortedMinWork)
+        (work >= gst::kSortedMinWork ||
+         (dim >= 2 && work >= gst::kSortedMinWorkPts && n_pts >= gst::kSortedMinPts)))
         return gst::summate_mixed_sorted(dim, n_modes, n_pts, cov_samples, z_1, z_2, pos,
                                          out, out_type == GST_OUT_F32 ? 1 : 0, 1.0,
                                          static_cast<cudaStream_t>(stream));

@@ -130,10 +130,11 @@ int gst_summate_f64_noalloc(int dim, int64_t n_modes, int64_t n_pts,
 /* ----------------------------------------------------------------------- */
 
 /* Same contract as gst_summate_f64; `out` is double (GST_OUT_F64) or float
- * (GST_OUT_F32).  dim in 1..3.  Sums of at least 1e9 mode-points with at
- * most 16384 modes run the sorted amplitude-phase path of the ensembles
- * (points sorted spatially, modes by |k|_1, one SFU cosine per mode and
- * point); smaller ones the pointwise kernel described above. */
+ * (GST_OUT_F32).  dim in 1..3.  Sums with at most 16384 modes and at least
+ * 1e9 mode-points, or in 2-D / 3-D at least 4e8 mode-points over at least
+ * 2e5 points, run the sorted amplitude-phase path of the ensembles (points
+ * sorted spatially, modes by |k|_1, one SFU cosine per mode and point);
+ * smaller ones the pointwise kernel described above. */
 int gst_summate_mixed(int dim, int64_t n_modes, int64_t n_pts,
                       const double *cov_samples, const double *z_1,
                       const double *z_2, const double *pos, void *out,

@@ -1,8 +1,9 @@
 """Mixed-precision summate of large unstructured point sets (the sorted
 amplitude-phase path of gst_summate_mixed) against the FP64 oracle.
 
-``gst_summate_mixed`` sends sums of at least 1e9 mode-points (and at most
-16 384 modes) through the path the ensembles use: points sorted spatially,
+``gst_summate_mixed`` sends sums of at least 1e9 mode-points, or in 2-D /
+3-D of at least 4e8 over at least 2e5 points (and at most 16 384 modes),
+through the path the ensembles use: points sorted spatially,
 modes by |k|_1, one SFU cosine per mode and point, per-warp origins, FP32
 phases where they stay small and the exact split turn reduction elsewhere.
 The cases cover the direct store (enough point tiles) and the mode range
@@ -42,13 +43,15 @@ CASES = [
     (2, 2000, 600_000, 500.0, 1.0e5, 10.0, False),  # far from the origin
     (2, 4000, 400_000, 500.0, 0.0, 5.0, True),      # heavy tail: exact chunks
     (3, 2048, 600_000, 300.0, 3.0e4, 20.0, True),
+    (2, 1000, 450_000, 400.0, 0.0, 10.0, False),     # 4.5e8 over 4.5e5 points
 ]
 
 
 @pytest.mark.parametrize("case", CASES)
 def test_sorted_mixed_path_vs_oracle(cuda_lib, case):
     dim, n_modes, n_pts, extent, offset, ls, heavy = case
-    assert n_modes * n_pts >= 1e9
+    assert n_modes * n_pts >= 1e9 or (dim >= 2 and n_modes * n_pts >= 4e8
+                                      and n_pts >= 200_000)
     rng = np.random.RandomState(n_modes + n_pts + dim)
     cov, z1, z2 = _modes(rng, dim, n_modes, ls, heavy)
     pos = offset + rng.uniform(0.0, extent, size=(dim, n_pts))
