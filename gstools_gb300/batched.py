@@ -31,7 +31,7 @@ import numpy as np
 import torch
 
 from . import _native
-from .summator import _finish, device
+from .summator import _finish, _host_concat, device
 
 __all__ = ["BatchedSummator", "VARIANTS"]
 
@@ -136,13 +136,25 @@ class BatchedSummator:
         self._staged = torch.cuda.Event()
         self._staged.record(stream)
 
-    def _fill_points(self, pos, xx):
-        for r in range(self.n_items):
-            p0, p1 = self.point_off[r], self.point_off[r + 1]
-            x = np.asarray(pos[r], dtype=np.float64).reshape(self.dim, -1)
-            if x.shape[1] != p1 - p0:
-                raise ValueError(f"realization {r}: sizes do not match the plan")
-            xx[:, p0:p1] = x
+    def _as_items(self, arrays, counts, what, flat=False):
+        """The per-realization arrays as float64 (dim, n) (or (n,)) arrays,
+        checked against the plan's sizes."""
+        out = []
+        for r, a in enumerate(arrays):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64):
+                a = np.asarray(a, dtype=np.float64)
+            a = a.reshape(-1) if flat else a.reshape(self.dim, -1)
+            if a.shape[-1] != counts[r]:
+                raise ValueError(f"realization {r}: {what} sizes do not match the plan")
+            out.append(a)
+        return out
+
+    def _fill_points(self, pos, xx, jobs=None):
+        """Copy the point sets (and the copies in `jobs`) into the staging
+        buffers, on the host's threads."""
+        jobs = [] if jobs is None else jobs
+        jobs.append((xx, self._as_items(pos, self.points, "point")))
+        _host_concat(jobs)
 
     def load_points(self, pos):
         """Copy the per-realization point sets (already isometrized, the
@@ -209,25 +221,22 @@ class BatchedSummator:
         z1_h = self._staging("z1", (self.total_modes,))
         z2_h = self._staging("z2", (self.total_modes,))
         xx_h = self._staging("pos", (self.dim, self.total_points))
-        cov, zz1, zz2 = cov_h.numpy(), z1_h.numpy(), z2_h.numpy()
-        for r in range(self.n_items):
-            m0, m1 = self.mode_off[r], self.mode_off[r + 1]
-            c = np.asarray(cov_samples[r], dtype=np.float64).reshape(self.dim, -1)
-            if c.shape[1] != m1 - m0:
-                raise ValueError(f"realization {r}: sizes do not match the plan")
-            cov[:, m0:m1] = c
-            zz1[m0:m1] = np.asarray(z_1[r], dtype=np.float64).reshape(-1)
-            zz2[m0:m1] = np.asarray(z_2[r], dtype=np.float64).reshape(-1)
-        self._fill_points(pos, xx_h.numpy())
-        self._upload([(self.cov, cov_h), (self.z1, z1_h), (self.z2, z2_h),
-                      (self.pos, xx_h)])
+        jobs = [(cov_h.numpy(), self._as_items(cov_samples, self.modes, "mode")),
+                (z1_h.numpy(), self._as_items(z_1, self.modes, "z_1", flat=True)),
+                (z2_h.numpy(), self._as_items(z_2, self.modes, "z_2", flat=True))]
+        uploads = [(self.cov, cov_h), (self.z1, z1_h), (self.z2, z2_h),
+                   (self.pos, xx_h)]
         if scales is not None:
             s = np.asarray(scales, dtype=np.float64).reshape(-1)
             if s.size != self.n_items:
                 raise ValueError("one scale per realization expected")
-            self.scales[: self.n_items].copy_(torch.from_numpy(s))
+            s_h = self._staging("scales", (self.n_items,))
+            s_h.numpy()[:] = s
+            uploads.append((self.scales[: self.n_items], s_h))
         else:
             self.scales.fill_(1.0)
+        self._fill_points(pos, xx_h.numpy(), jobs)
+        self._upload(uploads)
 
     def split(self, out=None):
         """Per-realization numpy views of a host copy of ``out`` (a pooled

@@ -20,7 +20,9 @@ isometrize matrix (``<k, M x> = <M^T k, x>``).
 """
 
 import ctypes
+import os
 import threading
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import torch
@@ -68,6 +70,96 @@ def _is_torch(*arrays):
     return any(isinstance(a, torch.Tensor) for a in arrays)
 
 
+_COPY_MIN_BYTES = 8 << 20     # host copies from this size on run on threads
+_COPY_PIECE_BYTES = 1 << 20
+_copy_pool = None
+_copy_lock = threading.Lock()
+
+
+def _host_copy(pairs):
+    """``dst[...] = src`` for every (dst, src) pair of numpy arrays of one
+    shape.  From 8 MiB in total the copies are cut into ~1 MiB pieces along
+    the last axis and run on a pool of host threads (numpy releases the GIL
+    while it copies): one core copies a few GB/s, the host's cores together
+    several times that, which is what feeding the GPU from host arrays
+    needs."""
+    total = sum(src.nbytes for _, src in pairs)
+    workers = min(16, os.cpu_count() or 1)
+    if total < _COPY_MIN_BYTES or workers < 2:
+        for dst, src in pairs:
+            dst[...] = src
+        return
+    global _copy_pool
+    with _copy_lock:
+        if _copy_pool is None:
+            _copy_pool = ThreadPoolExecutor(max_workers=workers,
+                                            thread_name_prefix="gst-copy")
+    # one task per worker, of about equal bytes (a task per piece would
+    # cost more in submissions than the copies take)
+    share = -(-total // workers)
+    tasks, cur, cur_bytes = [], [], 0
+    for dst, src in pairs:
+        n = src.shape[-1] if src.ndim else 1
+        col = max(1, src.nbytes // max(n, 1))
+        step = max(1, _COPY_PIECE_BYTES // col)
+        spans = [(a, min(a + step, n)) for a in range(0, n, step)] if src.ndim else [None]
+        for span in spans:
+            piece = (dst, src) if span is None else (dst[..., span[0]:span[1]],
+                                                    src[..., span[0]:span[1]])
+            cur.append(piece)
+            cur_bytes += piece[1].nbytes
+            if cur_bytes >= share:
+                tasks.append(cur)
+                cur, cur_bytes = [], 0
+    if cur:
+        tasks.append(cur)
+
+    def run(task):
+        for dst, src in task:
+            dst[...] = src
+
+    for f in [_copy_pool.submit(run, t) for t in tasks]:
+        f.result()
+
+
+def _host_concat(jobs):
+    """For every (dst, arrays) job, ``dst[...] = np.concatenate(arrays,
+    axis=-1)``.  From 8 MiB in total the arrays are cut into groups of about
+    equal bytes, one per host thread, each written by one np.concatenate
+    straight into its columns of dst (one Python call per group: a call per
+    array would serialise hundreds of small copies on the interpreter)."""
+    total = sum(a.nbytes for _, arrays in jobs for a in arrays)
+    workers = min(16, os.cpu_count() or 1)
+    if total < _COPY_MIN_BYTES or workers < 2:
+        for dst, arrays in jobs:
+            if arrays:
+                np.concatenate(arrays, axis=-1, out=dst)
+        return
+    global _copy_pool
+    with _copy_lock:
+        if _copy_pool is None:
+            _copy_pool = ThreadPoolExecutor(max_workers=workers,
+                                            thread_name_prefix="gst-copy")
+    share = -(-total // workers)
+    groups = []
+    for dst, arrays in jobs:
+        col, first, size = 0, 0, 0
+        start = 0
+        for i, a in enumerate(arrays):
+            size += a.nbytes
+            if size >= share or i == len(arrays) - 1:
+                width = sum(b.shape[-1] for b in arrays[first:i + 1])
+                groups.append((dst[..., start:start + width], arrays[first:i + 1]))
+                start += width
+                first, size = i + 1, 0
+
+    def run(group):
+        np.concatenate(group[1], axis=-1, out=group[0])
+
+    for f in [_copy_pool.submit(run, g) for g in groups]:
+        f.result()
+
+
 def _upload_host(arrays, dev):
     """Host arrays as float64 device tensors through ONE asynchronous copy
     from a pooled page-locked block (instead of a pageable copy each).
@@ -80,10 +172,11 @@ def _upload_host(arrays, dev):
     block = _PinnedBlock(total * 8)
     host = block.tensor.view(torch.float64)
     host_np = host.numpy()
-    off = 0
+    pairs, off = [], 0
     for f in flat:
-        host_np[off:off + f.size] = f.reshape(-1)
+        pairs.append((host_np[off:off + f.size], f.reshape(-1)))
         off += f.size
+    _host_copy(pairs)
     dbuf = torch.empty(total, dtype=torch.float64, device=dev)
     dbuf.copy_(host, non_blocking=True)
     out, off = [], 0
