@@ -361,4 +361,4 @@ def randmeth_field(cov_ref, len_scale_ref, z_1, z_2, pos=None, *, var, len_scale
         u = SummateGridFunction.apply(k, z_1, z_2, pos, tuple(axes), precision)
     else:
         u = summate_torch(k, z_1, z_2, pos, precision)
-    return torch.sqrt(var / n_modes) * u
+    return torch.sqrt(torch.as_tensor(var, dtype=torch.float64) / n_modes) * u
