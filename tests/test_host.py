@@ -242,27 +242,6 @@ def test_torch_isometrize_matches_numpy():
         np.testing.assert_allclose(got.numpy(), ref, rtol=0, atol=1e-15)
 
 
-def test_host_copy_threads_match_plain_copies():
-    """The threaded host copy (staging of large host inputs) writes exactly
-    what plain assignments write: strided 2-D destinations, 1-D pieces and
-    scalars, above and below the threading threshold."""
-    from gstools_gb300.summator import _host_copy
-
-    rng = np.random.RandomState(3)
-    for n in (1000, 700_001):
-        dst = np.zeros((3, 2 * n + 5))
-        srcs = [rng.normal(size=(3, n)), rng.normal(size=(3, n + 5))]
-        flat = np.zeros(n + 7)
-        fsrc = rng.normal(size=n + 7)
-        zero_d = np.zeros(())
-        _host_copy([(dst[:, :n], srcs[0]), (dst[:, n:], srcs[1]), (flat, fsrc),
-                    (zero_d, np.array(2.5))])
-        np.testing.assert_array_equal(dst[:, :n], srcs[0])
-        np.testing.assert_array_equal(dst[:, n:], srcs[1])
-        np.testing.assert_array_equal(flat, fsrc)
-        assert zero_d == 2.5
-
-
 def test_host_concat_threads_match_numpy():
     """The grouped threaded concatenation (ensemble staging) writes what
     np.concatenate writes, for 2-D and 1-D jobs with empty members, above
