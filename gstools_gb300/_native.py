@@ -40,6 +40,7 @@ SIGNATURES = {
     "gst_status_string": (ctypes.c_char_p, [_c_int]),
     "gst_last_cuda_error": (_c_int, []),
     "gst_read_device_error": (_c_int, [_ptr, ctypes.POINTER(_u32)]),
+    "gst_host_gather": (_c_int, [_i64, _ptr, _ptr, _i64, _ptr, _i64, _c_int]),
     "gst_summate_f64": (_c_int, [_c_int, _i64, _i64, _ptr, _ptr, _ptr, _ptr,
                                  _ptr, _ptr]),
     "gst_summate_f64_noalloc": (_c_int, [_c_int, _i64, _i64, _ptr, _ptr,

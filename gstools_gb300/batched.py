@@ -25,13 +25,14 @@ distributions are the models' spectral laws.
 
 import ctypes
 import hashlib
+import os
 import threading
 
 import numpy as np
 import torch
 
 from . import _native
-from .summator import _finish, _host_concat, device
+from .summator import _finish, device
 
 __all__ = ["BatchedSummator", "VARIANTS"]
 
@@ -137,24 +138,38 @@ class BatchedSummator:
         self._staged.record(stream)
 
     def _as_items(self, arrays, counts, what, flat=False):
-        """The per-realization arrays as float64 (dim, n) (or (n,)) arrays,
-        checked against the plan's sizes."""
+        """The per-realization arrays as C-contiguous float64 (dim, n) (or
+        (n,)) arrays, checked against the plan's sizes."""
         out = []
         for r, a in enumerate(arrays):
-            if not (isinstance(a, np.ndarray) and a.dtype == np.float64):
-                a = np.asarray(a, dtype=np.float64)
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64
+                    and a.flags.c_contiguous):
+                a = np.ascontiguousarray(a, dtype=np.float64)
             a = a.reshape(-1) if flat else a.reshape(self.dim, -1)
             if a.shape[-1] != counts[r]:
                 raise ValueError(f"realization {r}: {what} sizes do not match the plan")
             out.append(a)
         return out
 
+    @staticmethod
+    def _gather(dst, items, cols):
+        """``dst[...] = np.concatenate(items, axis=-1)`` by the library's
+        host gather (plain memcpy on the host's threads)."""
+        ptrs = np.fromiter((a.__array_interface__["data"][0] for a in items),
+                           dtype=np.uint64, count=len(items))
+        cols = np.ascontiguousarray(cols, dtype=np.int64)
+        rows = 1 if dst.ndim == 1 else dst.shape[0]
+        _native.call("gst_host_gather", len(items), ptrs.ctypes.data,
+                     cols.ctypes.data, rows, dst.ctypes.data, dst.shape[-1],
+                     min(16, os.cpu_count() or 1))
+
     def _fill_points(self, pos, xx, jobs=None):
-        """Copy the point sets (and the copies in `jobs`) into the staging
-        buffers, on the host's threads."""
+        """Copy the point sets (and the copies in `jobs`: (dst, items,
+        counts)) into the staging buffers."""
         jobs = [] if jobs is None else jobs
-        jobs.append((xx, self._as_items(pos, self.points, "point")))
-        _host_concat(jobs)
+        jobs.append((xx, self._as_items(pos, self.points, "point"), self.points))
+        for dst, items, counts in jobs:
+            self._gather(dst, items, counts)
 
     def load_points(self, pos):
         """Copy the per-realization point sets (already isometrized, the
@@ -221,9 +236,12 @@ class BatchedSummator:
         z1_h = self._staging("z1", (self.total_modes,))
         z2_h = self._staging("z2", (self.total_modes,))
         xx_h = self._staging("pos", (self.dim, self.total_points))
-        jobs = [(cov_h.numpy(), self._as_items(cov_samples, self.modes, "mode")),
-                (z1_h.numpy(), self._as_items(z_1, self.modes, "z_1", flat=True)),
-                (z2_h.numpy(), self._as_items(z_2, self.modes, "z_2", flat=True))]
+        jobs = [(cov_h.numpy(), self._as_items(cov_samples, self.modes, "mode"),
+                 self.modes),
+                (z1_h.numpy(), self._as_items(z_1, self.modes, "z_1", flat=True),
+                 self.modes),
+                (z2_h.numpy(), self._as_items(z_2, self.modes, "z_2", flat=True),
+                 self.modes)]
         uploads = [(self.cov, cov_h), (self.z1, z1_h), (self.z2, z2_h),
                    (self.pos, xx_h)]
         if scales is not None:

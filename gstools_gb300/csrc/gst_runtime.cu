@@ -1,6 +1,10 @@
 // Library-wide runtime pieces: version, status strings, per-device caches and
 // the device error word that bounded waits report into.
+#include <algorithm>
+#include <cstring>
 #include <mutex>
+#include <thread>
+#include <vector>
 
 #include "gst_common.cuh"
 
@@ -130,6 +134,53 @@ int gst_read_device_error(void *stream, uint32_t *device_error) {
     const unsigned int zero = 0;
     GST_TRY_CUDA(cudaMemcpyToSymbol(g_device_error_word, &zero, sizeof(zero)));
     *device_error = word;
+    return GST_OK;
+}
+
+int gst_host_gather(int64_t n_arrays, const uint64_t *src, const int64_t *cols,
+                    int64_t rows, double *dst, int64_t dst_cols, int threads) {
+    if (n_arrays < 0 || rows < 0 || dst_cols < 0) return GST_ERR_INVALID_ARGUMENT;
+    if (n_arrays == 0 || rows == 0 || dst_cols == 0) return GST_OK;
+    if (src == nullptr || cols == nullptr || dst == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    // column offset of every array in a row of dst
+    std::vector<int64_t> off(static_cast<size_t>(n_arrays) + 1, 0);
+    for (int64_t a = 0; a < n_arrays; ++a) {
+        if (cols[a] < 0 || (cols[a] > 0 && src[a] == 0)) return GST_ERR_INVALID_ARGUMENT;
+        off[a + 1] = off[a] + cols[a];
+    }
+    if (off[n_arrays] != dst_cols) return GST_ERR_INVALID_ARGUMENT;
+    const int64_t total = rows * dst_cols;   // elements of dst
+    // Thread t fills the elements [t total / n, (t + 1) total / n) of dst
+    // (row-major order): equal bytes per thread, contiguous writes.
+    auto fill = [&](int64_t lo, int64_t hi) {
+        while (lo < hi) {
+            const int64_t row = lo / dst_cols, c = lo % dst_cols;
+            const int64_t row_end = std::min(hi, (row + 1) * dst_cols);
+            // the array holding column c
+            int64_t a = std::upper_bound(off.begin(), off.end(), c) - off.begin() - 1;
+            int64_t col = c;
+            while (lo < row_end) {
+                while (off[a + 1] <= col) ++a;   // skip arrays without columns
+                const int64_t n = std::min(off[a + 1], col + (row_end - lo)) - col;
+                const double *from = reinterpret_cast<const double *>(src[a]) +
+                                     row * cols[a] + (col - off[a]);
+                std::memcpy(dst + lo, from, static_cast<size_t>(n) * sizeof(double));
+                lo += n;
+                col += n;
+            }
+        }
+    };
+    int n = std::max(1, std::min(threads, 64));
+    if (total * static_cast<int64_t>(sizeof(double)) < (4 << 20)) n = 1;
+    if (n == 1) {
+        fill(0, total);
+        return GST_OK;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(static_cast<size_t>(n));
+    for (int t = 0; t < n; ++t)
+        pool.emplace_back(fill, total * t / n, total * (t + 1) / n);
+    for (auto &th : pool) th.join();
     return GST_OK;
 }
 

@@ -20,9 +20,7 @@ isometrize matrix (``<k, M x> = <M^T k, x>``).
 """
 
 import ctypes
-import os
 import threading
-from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import torch
@@ -68,49 +66,6 @@ def _on_device(a, dev):
 
 def _is_torch(*arrays):
     return any(isinstance(a, torch.Tensor) for a in arrays)
-
-
-_COPY_MIN_BYTES = 8 << 20     # host copies from this size on run on threads
-_copy_pool = None
-_copy_lock = threading.Lock()
-
-
-def _host_concat(jobs):
-    """For every (dst, arrays) job, ``dst[...] = np.concatenate(arrays,
-    axis=-1)``.  From 8 MiB in total the arrays are cut into groups of about
-    equal bytes, one per host thread, each written by one np.concatenate
-    straight into its columns of dst (one Python call per group: a call per
-    array would serialise hundreds of small copies on the interpreter)."""
-    total = sum(a.nbytes for _, arrays in jobs for a in arrays)
-    workers = min(16, os.cpu_count() or 1)
-    if total < _COPY_MIN_BYTES or workers < 2:
-        for dst, arrays in jobs:
-            if arrays:
-                np.concatenate(arrays, axis=-1, out=dst)
-        return
-    global _copy_pool
-    with _copy_lock:
-        if _copy_pool is None:
-            _copy_pool = ThreadPoolExecutor(max_workers=workers,
-                                            thread_name_prefix="gst-copy")
-    share = -(-total // workers)
-    groups = []
-    for dst, arrays in jobs:
-        col, first, size = 0, 0, 0
-        start = 0
-        for i, a in enumerate(arrays):
-            size += a.nbytes
-            if size >= share or i == len(arrays) - 1:
-                width = sum(b.shape[-1] for b in arrays[first:i + 1])
-                groups.append((dst[..., start:start + width], arrays[first:i + 1]))
-                start += width
-                first, size = i + 1, 0
-
-    def run(group):
-        np.concatenate(group[1], axis=-1, out=group[0])
-
-    for f in [_copy_pool.submit(run, g) for g in groups]:
-        f.result()
 
 
 def _upload_host(arrays, dev):

@@ -72,6 +72,15 @@ int gst_last_cuda_error(void);
  * `stream`.  *device_error receives the word (0 = none). */
 int gst_read_device_error(void *stream, uint32_t *device_error);
 
+/* Host-side gather (no device work): n_arrays row-major float64 arrays of
+ * `rows` rows and cols[a] columns each (src[a] their addresses) side by
+ * side into the row-major rows x dst_cols array dst (dst_cols = sum of
+ * cols), on up to `threads` host threads -- one ensemble's per-realization
+ * inputs into its page-locked staging buffer.  No counterpart in the
+ * reference. */
+int gst_host_gather(int64_t n_arrays, const uint64_t *src, const int64_t *cols,
+                    int64_t rows, double *dst, int64_t dst_cols, int threads);
+
 /* ----------------------------------------------------------------------- */
 /* Plain FP64 pointwise kernels (parity anchors).                           */
 /* ----------------------------------------------------------------------- */

@@ -80,3 +80,30 @@ def test_tc_tile_width_choice(lib):
     for nz in range(1, 2000, 7):
         nt = lib.gst_grid_tc_tile_cols(nz)
         assert -(-nz // nt) * nt <= -(-nz // 256) * 256 or nt == 256, nz
+
+
+def test_host_gather_matches_concatenate(lib):
+    """gst_host_gather (host memcpy on threads, no device work) writes what
+    np.concatenate(axis=-1) writes: 2-D and 1-D, empty members, one thread
+    and many, above and below its threading threshold."""
+    import numpy as np
+
+    rng = np.random.RandomState(6)
+    for rows, scale in ((2, 1), (2, 3000), (1, 3000), (3, 7)):
+        cols = list(rng.randint(0, 50 * scale, size=33)) + [0, 5]
+        items = [np.ascontiguousarray(rng.normal(size=(rows, c))) for c in cols]
+        dst = np.zeros((rows, sum(cols)))
+        ptrs = np.array([a.__array_interface__["data"][0] for a in items],
+                        dtype=np.uint64)
+        cc = np.array(cols, dtype=np.int64)
+        for threads in (1, 7):
+            dst[...] = 0.0
+            rc = lib.gst_host_gather(len(items), ptrs.ctypes.data, cc.ctypes.data,
+                                     rows, dst.ctypes.data, dst.shape[1], threads)
+            assert rc == 0
+            np.testing.assert_array_equal(dst, np.concatenate(items, axis=-1))
+    # column counts that do not add up to the destination are refused
+    cc = np.array([3, 4], dtype=np.int64)
+    ptrs = np.array([1, 1], dtype=np.uint64)
+    assert lib.gst_host_gather(2, ptrs.ctypes.data, cc.ctypes.data, 1,
+                               dst.ctypes.data, 8, 1) == _native.GST_ERR_INVALID_ARGUMENT

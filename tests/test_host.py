@@ -240,21 +240,3 @@ def test_torch_isometrize_matches_numpy():
         got = isometrize_matrix(dim, torch.tensor(angles, dtype=torch.float64),
                                 torch.tensor(anis, dtype=torch.float64))
         np.testing.assert_allclose(got.numpy(), ref, rtol=0, atol=1e-15)
-
-
-def test_host_concat_threads_match_numpy():
-    """The grouped threaded concatenation (ensemble staging) writes what
-    np.concatenate writes, for 2-D and 1-D jobs with empty members, above
-    and below the threading threshold."""
-    from gstools_gb300.summator import _host_concat
-
-    rng = np.random.RandomState(4)
-    for scale in (1, 400):
-        sizes = list(rng.randint(0, 50 * scale, size=40)) + [0, 3]
-        pts = [rng.normal(size=(2, n)) for n in sizes]
-        zs = [rng.normal(size=n) for n in sizes]
-        dst2 = np.zeros((2, sum(sizes)))
-        dst1 = np.zeros(sum(sizes))
-        _host_concat([(dst2, pts), (dst1, zs)])
-        np.testing.assert_array_equal(dst2, np.concatenate(pts, axis=-1))
-        np.testing.assert_array_equal(dst1, np.concatenate(zs))
