@@ -22,6 +22,8 @@ LIB_NAME = "libgstools_gb300.so"
 LIB_PATH = os.path.join(PKG_DIR, LIB_NAME)
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# cuBLAS runs the plain FP16 slice GEMMs of the FP64 kriging variance
+LINK_LIBS = ["-lcublas"]
 NVCC_FLAGS = [
     "-O3",
     "-lineinfo",
@@ -99,7 +101,7 @@ def build(force=False, verbose=False, ptxas_info=False, jobs=None):
             sys.stdout.write(log)
     objs = [o for o, _ in results]
     tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc_path(), *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
+    cmd = [nvcc_path(), *ARCH_FLAGS, "-shared", "-o", tmp, *objs, *LINK_LIBS]
     proc = subprocess.run(cmd, capture_output=True, text=True)
     if proc.returncode != 0:
         raise RuntimeError(f"link failed:\n{proc.stdout}\n{proc.stderr}")

@@ -19,8 +19,10 @@ unsigned int *g_error_word[kMaxDevices];
 cudaMemPool_t g_scratch_pool[kMaxDevices];
 bool g_scratch_pool_tried[kMaxDevices];
 cudaStream_t g_copy_stream[kMaxDevices];
-// Freed scratch the library's pool keeps mapped for the next call.
-constexpr uint64_t kScratchKeepBytes = 1ull << 30;
+// Freed scratch the library's pool keeps mapped for the next call (the
+// largest single user, the sliced kriging variance, takes ~2.5 GB for
+// 1000 conditions x 65 536 targets).
+constexpr uint64_t kScratchKeepBytes = 4ull << 30;
 thread_local cudaError_t g_last_cuda_error = cudaSuccess;
 
 }  // namespace

@@ -123,3 +123,60 @@ def test_kernel_torch_and_empty(cuda_lib):
     assert _within(f.cpu().numpy(), fo, scale)
     z = gg.calc_field_krige(np.zeros((0, 0)), np.zeros((0, 9)), np.zeros(0))
     np.testing.assert_array_equal(z, np.zeros(9))
+
+
+def _gauss_kriging_system(rng, k, n, dim=2, ls=3.0, nugget=1e-6):
+    """Inverted simple-kriging matrix of a Gaussian covariance (smooth,
+    ill-conditioned) and the target covariances, as the reference builds
+    them (krige/base.py:280-320)."""
+    cond_pos = rng.uniform(0.0, 20.0, size=(k, dim))
+    tgt_pos = rng.uniform(0.0, 20.0, size=(n, dim))
+
+    def cov(a, b):
+        d2 = ((a[:, None, :] - b[None, :, :]) ** 2).sum(-1)
+        return np.exp(-d2 / ls ** 2)
+
+    mat = np.linalg.inv(cov(cond_pos, cond_pos) + nugget * np.eye(k))
+    vecs = np.ascontiguousarray(cov(cond_pos, tgt_pos))
+    return mat, vecs, rng.normal(size=k)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["random", "kriging"])
+def test_sliced_variance_matches_oracle(cuda_lib, kind):
+    """Large K^2 n variances run as FP16 tensor-core products of error-free
+    FP64 slices: same scale-aware FP64 bar against the oracle."""
+    rng = np.random.RandomState(17 if kind == "random" else 18)
+    k, n = 1001, 4096
+    if kind == "random":
+        a = rng.normal(size=(k, k))
+        mat = a @ a.T / k + np.eye(k)
+        vecs = rng.normal(size=(k, n)) * np.exp(rng.uniform(-20, 20, size=(1, n)))
+        cond = rng.normal(size=k)
+    else:
+        mat, vecs, cond = _gauss_kriging_system(rng, k, n)
+    assert k * k * n >= 4e9
+    f, e = gg.calc_field_krige_and_variance(mat, vecs, cond)
+    fo, eo = oracle.c_krige(mat, vecs, cond)
+    _, _, scale = oracle.np_krige(mat, vecs, cond)
+    assert _within(f, fo, scale)
+    assert _within(e, eo, scale), np.max(np.abs(e - eo) / scale)
+    again = gg.calc_field_krige_and_variance(mat, vecs, cond)[1]
+    np.testing.assert_array_equal(e, again)   # deterministic
+
+
+@pytest.mark.gpu
+def test_sliced_variance_non_finite(cuda_lib):
+    rng = np.random.RandomState(19)
+    k, n = 1001, 4096
+    a = rng.normal(size=(k, k))
+    mat = a @ a.T / k + np.eye(k)
+    vecs = rng.normal(size=(k, n))
+    cond = rng.normal(size=k)
+    vecs[5, 7] = np.nan
+    e = gg.calc_field_krige_and_variance(mat, vecs, cond)[1]
+    assert np.isnan(e[7]) and np.isfinite(np.delete(e, 7)).all()
+    vecs[5, 7] = 1.0
+    mat[3, 4] = np.inf
+    e = gg.calc_field_krige_and_variance(mat, vecs, cond)[1]
+    assert np.isnan(e).all()
