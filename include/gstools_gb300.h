@@ -373,8 +373,12 @@ int gst_philox4x64_fill(uint64_t key0, uint64_t key1, int64_t n_blocks,
 /*   field[k] = sum_i cond[i] (M v_k)_i,  error[k] = sum_i v_ik (M v_k)_i    */
 /* error may be NULL for the field only, computed as field = V^T (M^T c):   */
 /* n_cond^2 + n_cond n_pts flops instead of n_cond^2 n_pts, same FP64 error */
-/* bound, n_cond doubles of stream-ordered scratch.  Device pointers; FP64; */
-/* deterministic.                                                           */
+/* bound, n_cond doubles of stream-ordered scratch.  Variances with         */
+/* n_cond <= 4096 and n_cond^2 n_pts >= 4e9 form M V from error-free FP16   */
+/* slices on the tensor cores (exact slice products, FP64 folds; FP64-level */
+/* accuracy; a non-finite value in M makes every error NaN, one in column k */
+/* of V error[k]), with ~(9 x 2 + 20) n_cond n_pts bytes of scratch.         */
+/* Device pointers; FP64; deterministic.                                    */
 /* ----------------------------------------------------------------------- */
 int gst_calc_field_krige(int64_t n_cond, int64_t n_pts, const double *krig_mat,
                          const double *krig_vecs, const double *cond, double *field,
