@@ -377,7 +377,7 @@ int gst_philox4x64_fill(uint64_t key0, uint64_t key1, int64_t n_blocks,
 /* n_cond <= 4096 and n_cond^2 n_pts >= 4e9 form M V from error-free FP16   */
 /* slices on the tensor cores (exact slice products, FP64 folds; FP64-level */
 /* accuracy; a non-finite value in M makes every error NaN, one in column k */
-/* of V error[k]), with ~(9 x 2 + 20) n_cond n_pts bytes of scratch.         */
+/* of V error[k]), with ~34 n_cond n_pts bytes of scratch.                 */
 /* Device pointers; FP64; deterministic.                                    */
 /* ----------------------------------------------------------------------- */
 int gst_calc_field_krige(int64_t n_cond, int64_t n_pts, const double *krig_mat,
