@@ -26,6 +26,8 @@
 #include <algorithm>
 #include <climits>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "gst_common.cuh"
 
@@ -199,6 +201,9 @@ constexpr int64_t kOzakiMaxInner = (int64_t(1) << 24) >> (2 * kBeta);   // 4096
 // Largest magnitude of slice s: 2^kBeta for the first, 2^(kBeta-1) after
 // (the remainders of rint are at most 1/2).
 constexpr int64_t slice_bound(int s) { return s == 1 ? (1 << kBeta) : (1 << (kBeta - 1)); }
+// Lowest level accumulated in FP32 (see krige_variance_ozaki).
+constexpr int kChainLevel = 7;
+static_assert(24 + kBeta * (kChainLevel - 2) >= 53, "FP32 chain above FP64 resolution");
 
 // Exponent a with |x| < 2^a for the largest |x| of row i (thread-per-row
 // warps: one warp per row); a non-finite value sets *bad.
@@ -451,20 +456,22 @@ int krige_variance_ozaki(int64_t K, int64_t n, const double *mat, const double *
     GST_TRY_CUDA(fe.create());
     GST_TRY_CUDA(cudaEventRecord(fe.ev[4], s));
     GST_TRY_CUDA(cudaStreamWaitEvent(side, fe.ev[4], 0));
-    const float one = 1.0f, zero = 0.0f;
+    const float one = 1.0f;
     bool first = true;
-    int gi = 0;   // GEMMs issued
+    int gi = 0;           // GEMMs issued
+    int last_fold = -1;   // buffer of the last fold queued
     // on a failure after folds were queued, s still waits for them: the
     // scratch they use is released on s
     auto bail = [&](int code) {
-        if (gi > 0) cudaStreamWaitEvent(s, fe.ev[2 + ((gi - 1) & 1)], 0);
+        if (last_fold >= 0) cudaStreamWaitEvent(s, fe.ev[2 + last_fold], 0);
         return code;
     };
-    for (int L = 2; L <= kSlices + 1; ++L) {
+    // The GEMM groups of level L: as many pairs as keep every sum an integer
+    // below 2^24 (Kp sum_pairs |q_s| |q_t| <= 2^24).
+    auto groups_of = [&](int L) {
+        std::vector<std::pair<int, int>> g;
         const int s_lo = std::max(1, L - kSlices), s_hi = std::min(kSlices, L - 1);
-        for (int s1 = s_lo, s2 = s_lo; s1 <= s_hi; s1 = s2 + 1) {
-            // as many pairs of the level as keep every sum of the GEMM an
-            // integer below 2^24: Kp sum_pairs |q_s| |q_t| <= 2^24
+        for (int s1 = s_lo, s2; s1 <= s_hi; s1 = s2 + 1) {
             int64_t bound = slice_bound(s1) * slice_bound(L - s1);
             s2 = s1;
             while (s2 + 1 <= s_hi &&
@@ -473,40 +480,75 @@ int krige_variance_ozaki(int64_t K, int64_t n, const double *mat, const double *
                 ++s2;
                 bound += slice_bound(s2) * slice_bound(L - s2);
             }
-            const int64_t inner = static_cast<int64_t>(s2 - s1 + 1) * Kp;
-            // row-major P (K x np) = QM[:, s1..s2 blocks] (K x inner) times
-            // QV[rows of t = L - s1 .. L - s2] (inner x np); cuBLAS sees the
-            // column-major transposes: P^T = QV^T QM^T
-            const __half *a = qv + static_cast<int64_t>(kSlices - L + s1) * Kp * np;
-            const __half *b = qm + static_cast<int64_t>(s1 - 1) * Kp;
-            const int buf = gi & 1;
-            float *pb = p + static_cast<int64_t>(buf) * K * np;
-            if (gi >= 2 && cudaStreamWaitEvent(s, fe.ev[2 + buf], 0) != cudaSuccess)
-                return bail(GST_ERR_CUDA);
-            if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, static_cast<int>(np),
-                             static_cast<int>(K), static_cast<int>(inner), &one, a,
-                             CUDA_R_16F, static_cast<int>(np), b, CUDA_R_16F,
-                             static_cast<int>(kSlices * Kp), &zero, pb, CUDA_R_32F,
-                             static_cast<int>(np), CUBLAS_COMPUTE_32F,
-                             CUBLAS_GEMM_DEFAULT) != CUBLAS_STATUS_SUCCESS)
-                return bail(GST_ERR_CUDA);
-            if (cudaEventRecord(fe.ev[buf], s) != cudaSuccess ||
-                cudaStreamWaitEvent(side, fe.ev[buf], 0) != cudaSuccess)
-                return bail(GST_ERR_CUDA);
-            fold_kernel<64, 4><<<static_cast<unsigned>(ceil_div(n, 64)), 256, 0, side>>>(
-                K, n, np, vsc, pb, ldexp(1.0, -kBeta * L), first ? 1 : 0, d);
-            if (cudaGetLastError() != cudaSuccess ||
-                cudaEventRecord(fe.ev[2 + buf], side) != cudaSuccess) {
-                ++gi;
-                return bail(GST_ERR_CUDA);
-            }
-            first = false;
-            ++gi;
+            g.emplace_back(s1, s2);
+        }
+        return g;
+    };
+    bool pending[2] = {false, false};   // a fold still reads this buffer
+    // P[buf] = QM[:, s1..s2 blocks] QV[rows of t = L - s1 .. L - s2]
+    // (+ beta P[buf]); row-major, so cuBLAS sees the column-major
+    // transposes: P^T = QV^T QM^T
+    auto gemm = [&](int L, int s1, int s2, float beta, int buf) -> int {
+        const int64_t inner = static_cast<int64_t>(s2 - s1 + 1) * Kp;
+        const __half *a = qv + static_cast<int64_t>(kSlices - L + s1) * Kp * np;
+        const __half *b = qm + static_cast<int64_t>(s1 - 1) * Kp;
+        float *pb = p + static_cast<int64_t>(buf) * K * np;
+        if (pending[buf] && cudaStreamWaitEvent(s, fe.ev[2 + buf], 0) != cudaSuccess)
+            return GST_ERR_CUDA;
+        pending[buf] = false;
+        if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, static_cast<int>(np),
+                         static_cast<int>(K), static_cast<int>(inner), &one, a,
+                         CUDA_R_16F, static_cast<int>(np), b, CUDA_R_16F,
+                         static_cast<int>(kSlices * Kp), &beta, pb, CUDA_R_32F,
+                         static_cast<int>(np), CUBLAS_COMPUTE_32F,
+                         CUBLAS_GEMM_DEFAULT) != CUBLAS_STATUS_SUCCESS)
+            return GST_ERR_CUDA;
+        ++gi;
+        return GST_OK;
+    };
+    // d (+)= 2^(-kBeta L) sum_i vs_ik P[buf]_ik on `side`, after the GEMMs
+    auto fold = [&](int L, int buf) -> int {
+        if (cudaEventRecord(fe.ev[buf], s) != cudaSuccess ||
+            cudaStreamWaitEvent(side, fe.ev[buf], 0) != cudaSuccess)
+            return GST_ERR_CUDA;
+        fold_kernel<64, 4><<<static_cast<unsigned>(ceil_div(n, 64)), 256, 0, side>>>(
+            K, n, np, vsc, p + static_cast<int64_t>(buf) * K * np, ldexp(1.0, -kBeta * L),
+            first ? 1 : 0, d);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaEventRecord(fe.ev[2 + buf], side) != cudaSuccess)
+            return GST_ERR_CUDA;
+        pending[buf] = true;
+        last_fold = buf;
+        first = false;
+        return GST_OK;
+    };
+    // Levels kChainLevel..S+1 accumulate in FP32, each new level scaling the
+    // sum so far by 2^-kBeta (beta of the GEMM): the rounding, at most
+    // 2^-24 of a level-kChainLevel term, lies below FP64 resolution
+    // relative to the leading level 2 (2^-24 2^(-kBeta (kChainLevel - 2))
+    // <= 2^-53); one fold takes them all.  The levels below are exact
+    // integer GEMMs, one fold each.
+    bool started = false;
+    for (int L = kSlices + 1; L >= kChainLevel; --L) {
+        bool level_first = true;
+        for (const auto &g : groups_of(L)) {
+            const float beta = !started ? 0.0f : (level_first ? 1.0f / (1 << kBeta) : 1.0f);
+            if (gemm(L, g.first, g.second, beta, 0)) return bail(GST_ERR_CUDA);
+            started = true;
+            level_first = false;
         }
     }
+    if (started && fold(kChainLevel, 0)) return bail(GST_ERR_CUDA);
+    int buf = 1;
+    for (int L = kChainLevel - 1; L >= 2; --L)
+        for (const auto &g : groups_of(L)) {
+            if (gemm(L, g.first, g.second, 0.0f, buf) || fold(L, buf))
+                return bail(GST_ERR_CUDA);
+            buf ^= 1;
+        }
     // every fold done (they run in order on `side`) before the result and
     // before the scratch is released on s
-    GST_TRY_CUDA(cudaStreamWaitEvent(s, fe.ev[2 + ((gi - 1) & 1)], 0));
+    if (last_fold >= 0) GST_TRY_CUDA(cudaStreamWaitEvent(s, fe.ev[2 + last_fold], 0));
     ozaki_finish_kernel<<<static_cast<unsigned>(ceil_div(n, 256)), 256, 0, s>>>(n, d, ce,
                                                                                 bad, error);
     GST_TRY_CUDA(cudaGetLastError());
