@@ -91,6 +91,7 @@ SIGNATURES = {
     "gst_summate_vjp_pos_f64": (_c_int, [_c_int, _i64, _i64] + [_ptr] * 6),
     "gst_summate_vjp_pos_mixed": (_c_int, [_c_int, _i64, _i64] + [_ptr] * 6),
     "gst_gather_points": (_c_int, [_c_int, _ptr, _ptr, _i64, _ptr, _i64] + [_ptr] * 5),
+    "gst_mode_map": (_c_int, [_c_int, _ptr, _dbl, _ptr, _ptr, _ptr]),
     "gst_grid_tc_contract_rows": (_c_int, [_c_int, _i64, _ptr, _ptr,
                                            ctypes.c_size_t, _ptr, _c_int, _dbl,
                                            _i64, _i64, _ptr]),

@@ -273,6 +273,87 @@ int run_vjp_modes(int prec, int dim, int64_t n_modes, int64_t n_pts,
     return GST_OK;
 }
 
+// The mode map of a differentiable field: mt = M(angles, anis)^T
+// (len_scale_ref / len_scale) with M = diag(1, 1/anis) R_0 R_1 ..., R_i the
+// Givens rotation of plane i ((0,1), (0,2), (1,2)) by (-1)^i (-angles_i) --
+// the reference's isometrize construction (src/gstools/tools/geometric.py:
+// 184-294) -- and its Jacobian jac[a][p] = d mt_a / d params_p (a = row-major
+// index of mt), params = [len_scale, anis..., angles...].  One thread: dim
+// <= 3, a few hundred flops.
+__device__ void mat3_mul(const double (&a)[3][3], const double (&b)[3][3], double (&c)[3][3]) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double t = 0.0;
+            for (int k = 0; k < 3; ++k) t += a[i][k] * b[k][j];
+            c[i][j] = t;
+        }
+}
+
+__global__ void mode_map_kernel(int dim, const double *__restrict__ params,
+                                double len_scale_ref, double *mt, double *jac) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int n_anis = dim - 1, n_ang = dim * (dim - 1) / 2;
+    const int n_par = 1 + n_anis + n_ang;
+    const double ls = params[0];
+    const double r = len_scale_ref / ls;
+    // Givens factors and their derivatives (3 x 3, identity beyond dim)
+    double g[3][3][3], dg[3][3][3];
+    int planes[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int i = 0; i < n_ang; ++i) {
+        const double th = ((i & 1) ? 1.0 : -1.0) * params[1 + n_anis + i];
+        const double c = cos(th), sn = sin(th);
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                g[i][a][b] = a == b ? 1.0 : 0.0;
+                dg[i][a][b] = 0.0;
+            }
+        const int p = planes[i][0], q = planes[i][1];
+        g[i][p][p] = g[i][q][q] = c;
+        g[i][p][q] = -sn;
+        g[i][q][p] = sn;
+        dg[i][p][p] = dg[i][q][q] = -sn;
+        dg[i][p][q] = -c;
+        dg[i][q][p] = c;
+    }
+    auto product = [&](int skip, double (&out)[3][3]) {
+        // G_0 ... G_{n-1} with factor `skip` replaced by its derivative
+        double acc[3][3], tmp[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) acc[a][b] = a == b ? 1.0 : 0.0;
+        for (int i = 0; i < n_ang; ++i) {
+            mat3_mul(acc, i == skip ? dg[i] : g[i], tmp);
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) acc[a][b] = tmp[a][b];
+        }
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) out[a][b] = acc[a][b];
+    };
+    double rot[3][3];
+    product(-1, rot);
+    double st[3] = {1.0, 1.0, 1.0};
+    for (int j = 0; j < n_anis; ++j) st[j + 1] = 1.0 / params[1 + j];
+    // mt[a][b] = M[b][a] r = st[b] rot[b][a] r
+    for (int a = 0; a < dim; ++a)
+        for (int b = 0; b < dim; ++b) {
+            const double v = st[b] * rot[b][a] * r;
+            mt[a * dim + b] = v;
+            jac[(a * dim + b) * n_par + 0] = -v / ls;   // d / d len_scale
+        }
+    for (int j = 0; j < n_anis; ++j)   // d / d anis_j: row j + 1 of M
+        for (int a = 0; a < dim; ++a)
+            for (int b = 0; b < dim; ++b)
+                jac[(a * dim + b) * n_par + 1 + j] =
+                    b == j + 1 ? -rot[b][a] * r / (params[1 + j] * params[1 + j]) : 0.0;
+    for (int i = 0; i < n_ang; ++i) {   // d / d angles_i
+        double drot[3][3];
+        product(i, drot);
+        const double dth = (i & 1) ? 1.0 : -1.0;
+        for (int a = 0; a < dim; ++a)
+            for (int b = 0; b < dim; ++b)
+                jac[(a * dim + b) * n_par + 1 + n_anis + i] = st[b] * drot[b][a] * r * dth;
+    }
+}
+
 struct GatherGeom {
     int dim;
     int64_t n[3];     // grid axis lengths
@@ -310,6 +391,17 @@ __global__ void gather_points_kernel(GatherGeom gg, const double *__restrict__ a
 }  // namespace gst
 
 extern "C" {
+
+int gst_mode_map(int dim, const double *params, double len_scale_ref, double *mt,
+                 double *jac, void *stream) {
+    if (dim < 1 || dim > 3) return GST_ERR_UNSUPPORTED_DIM;
+    if (params == nullptr || mt == nullptr || jac == nullptr) return GST_ERR_INVALID_ARGUMENT;
+    if (gst::current_device() < 0) return GST_ERR_NO_DEVICE;
+    gst::mode_map_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(
+        dim, params, len_scale_ref, mt, jac);
+    GST_TRY_CUDA(cudaGetLastError());
+    return GST_OK;
+}
 
 int gst_gather_points(int dim, const int64_t *axis_len, const double *axes,
                       int64_t n_extra, const double *x_extra, int64_t n_idx,

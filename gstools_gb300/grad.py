@@ -329,6 +329,29 @@ class _ModeMap(torch.autograd.Function):
         return torch.from_numpy(grad), None, None
 
 
+class _ModeMapDevice(torch.autograd.Function):
+    """The same map on the device (``gst_mode_map``: one kernel that also
+    writes the Jacobian d mt / d params), for parameters that live there:
+    no host round trip in the forward or the backward (the backward is
+    ``jac^T vec(grad)``)."""
+
+    @staticmethod
+    def forward(ctx, packed, dim, len_scale_ref):
+        prm = packed.detach().to(torch.float64).contiguous()
+        mt = torch.empty((dim, dim), dtype=torch.float64, device=prm.device)
+        jac = torch.empty((dim * dim, prm.numel()), dtype=torch.float64,
+                          device=prm.device)
+        _native.call("gst_mode_map", dim, _p(prm), float(len_scale_ref), _p(mt),
+                     _p(jac), _stream(prm.device))
+        ctx.save_for_backward(jac)
+        return mt
+
+    @staticmethod
+    def backward(ctx, grad_mt):
+        (jac,) = ctx.saved_tensors
+        return jac.T @ grad_mt.reshape(-1).to(jac.dtype), None, None
+
+
 def randmeth_field(cov_ref, len_scale_ref, z_1, z_2, pos=None, *, var, len_scale,
                    anis, angles, precision=None, axes=None):
     """Field at physical positions ``pos`` (dim, n) and/or on the
@@ -341,21 +364,21 @@ def randmeth_field(cov_ref, len_scale_ref, z_1, z_2, pos=None, *, var, len_scale
     if pos is None and axes is None:
         raise ValueError("give pos, axes or both")
     dim, n_modes = cov_ref.shape
-    # The dim x dim map M^T (len_scale_ref / len_scale) is built on the host
-    # from one host copy of the small parameters (differentiable: autograd
-    # copies their gradients back), so its few dozen scalar operations and
-    # their backward are no device launches; one dim x dim @ dim x N product
-    # runs on the device.
+    # The dim x dim map M^T (len_scale_ref / len_scale) and its derivative
+    # come from one kernel when the small parameters live on a CUDA device,
+    # else from numpy on the host; either way no chain of scalar autograd
+    # nodes, and one dim x dim @ dim x N product on the device.
     small = [torch.as_tensor(t, dtype=torch.float64).reshape(-1)
              for t in (len_scale, anis, angles)]
-    devs = {t.device for t in small}
-    if len(devs) == 1:
-        host = torch.cat(small).to("cpu")
-    else:
-        host = torch.cat([t.to("cpu") for t in small])
     if small[1].numel() != dim - 1 or small[2].numel() != dim * (dim - 1) // 2:
         raise ValueError("need dim - 1 anisotropy ratios and dim (dim - 1) / 2 angles")
-    mt = _ModeMap.apply(host, dim, float(len_scale_ref))
+    devs = {t.device for t in small}
+    dev0 = next(iter(devs))
+    if len(devs) == 1 and dev0.type == "cuda":
+        mt = _ModeMapDevice.apply(torch.cat(small), dim, float(len_scale_ref))
+    else:
+        host = torch.cat([t.to("cpu") for t in small])
+        mt = _ModeMap.apply(host, dim, float(len_scale_ref))
     k = mt.to(device=cov_ref.device, dtype=cov_ref.dtype) @ cov_ref
     if axes is not None:
         u = SummateGridFunction.apply(k, z_1, z_2, pos, tuple(axes), precision)

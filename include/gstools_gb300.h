@@ -288,6 +288,15 @@ int gst_summate_vjp_pos_mixed(int dim, int64_t n_modes, int64_t n_pts,
  * coordinates and gs (n_idx,) = g[idx] their cotangents -- the inputs of
  * gst_summate_vjp_* for the points of a field with a nonzero cotangent.
  * An index outside [0, grid points + n_extra) gives zeros. */
+/* The mode map of a differentiable RandMeth field, on the device (no host
+ * round trip): mt (dim x dim, row-major) = M^T len_scale_ref / len_scale
+ * with M the reference's isometrize matrix (src/gstools/tools/geometric.py:
+ * 184-294: Givens rotations of the planes (0,1), (0,2), (1,2) by
+ * (-1)^i (-angles_i), then diag(1, 1/anis)), and jac (dim^2 x n_params,
+ * row-major) = d mt / d params, params = [len_scale, anis (dim - 1),
+ * angles (dim (dim - 1) / 2)] (device).  The wave vectors are mt @ k_ref. */
+int gst_mode_map(int dim, const double *params, double len_scale_ref, double *mt,
+                 double *jac, void *stream);
 int gst_gather_points(int dim, const int64_t *axis_len, const double *axes,
                       int64_t n_extra, const double *x_extra, int64_t n_idx,
                       const int64_t *idx, const double *g, double *xs,

@@ -265,3 +265,25 @@ def test_gather_points_kernel(cuda_lib):
     assert torch.equal(xs[:, :6], allx[:, good])
     assert torch.equal(gs[:6], g[good])
     assert torch.all(xs[:, 6:] == 0) and torch.all(gs[6:] == 0)
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_device_mode_map_matches_host(cuda_lib, dim):
+    """gst_mode_map (map and Jacobian on the device) against the host map
+    and its analytic derivative."""
+    from gstools_gb300.grad import _ModeMap, _ModeMapDevice
+
+    rng = np.random.RandomState(40 + dim)
+    n_anis, n_ang = dim - 1, dim * (dim - 1) // 2
+    for _ in range(4):
+        vals = np.concatenate([[rng.uniform(2.0, 40.0)], rng.uniform(0.2, 3.0, n_anis),
+                               rng.uniform(-3.0, 3.0, n_ang)])
+        weight = torch.tensor(rng.normal(size=(dim, dim)))
+        host = torch.tensor(vals, requires_grad=True)
+        dev = torch.tensor(vals, device="cuda", requires_grad=True)
+        mh = _ModeMap.apply(host, dim, 13.0)
+        md = _ModeMapDevice.apply(dev, dim, 13.0)
+        assert torch.allclose(md.cpu(), mh, rtol=0, atol=1e-14)
+        (mh * weight).sum().backward()
+        (md * weight.cuda()).sum().backward()
+        assert torch.allclose(dev.grad.cpu(), host.grad, rtol=1e-12, atol=1e-14)
