@@ -198,15 +198,15 @@ constexpr int kBeta = 6;      // bits per slice
 constexpr int kSlices = 9;    // kBeta (kSlices + 1) = 60 bits
 constexpr int64_t kOzakiMaxInner = (int64_t(1) << 24) >> (2 * kBeta);   // 4096
 
-// Largest magnitude of slice s: 2^kBeta for the first, 2^(kBeta-1) after
-// (the remainders of rint are at most 1/2).
+// Largest magnitude of slice s: 2^kBeta for the leading digit, 2^(kBeta-1)
+// for the balanced digits after it (slice_digits).
 constexpr int64_t slice_bound(int s) { return s == 1 ? (1 << kBeta) : (1 << (kBeta - 1)); }
 // Lowest level accumulated in FP32 (see krige_variance_ozaki).
 constexpr int kChainLevel = 7;
 static_assert(24 + kBeta * (kChainLevel - 2) >= 53, "FP32 chain above FP64 resolution");
 
-// Exponent a with |x| < 2^a for the largest |x| of row i (thread-per-row
-// warps: one warp per row); a non-finite value sets *bad.
+// Exponent a with |x| < 2^a for the largest |x| of row i (one warp per
+// row) and the scale 2^a; a non-finite value sets *bad.
 __global__ void row_exponent_kernel(int64_t K, const double *__restrict__ m, int *expo,
                                     double *scale, unsigned int *bad) {
     const int64_t i = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
