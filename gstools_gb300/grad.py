@@ -4,6 +4,10 @@
 (``gst_summate_vjp_modes_*`` for dL/dz_1, dL/dz_2, dL/dk and
 ``gst_summate_vjp_pos_*`` for dL/dx; include/gstools_gb300.h).  The forward
 stores only its inputs; the backward recomputes sin/cos.
+:class:`SummateGridFunction` does the same for a structured grid (given by
+its axes, forward on the tensor cores in mixed precision), optionally
+followed by scattered points; its backward gathers the grid points with a
+nonzero cotangent (``gst_gather_points``) into one adjoint call.
 
 :func:`isometrize_matrix` rebuilds the reference's isometrize map
 (src/gstools/tools/geometric.py:184-294: derotation by Givens rotations with
@@ -18,6 +22,9 @@ with M = isometrize_matrix(angles, anis) and k(len_scale) = k_ref *
 (len_scale_ref / len_scale) -- the radial law of every model scales its wave
 numbers by 1 / len_rescaled (covmodel/models.py:143-186, 226-270), so
 gradients reach len_scale, the anisotropy ratios and the rotation angles.
+The map M^T len_scale_ref / len_scale and its Jacobian come from one device
+kernel (``gst_mode_map``) for parameters on the GPU, from numpy for host
+parameters.
 """
 
 import ctypes
