@@ -159,27 +159,33 @@ class SummateGridFunction(torch.autograd.Function):
         ax = [_dev_f64(torch.as_tensor(a), dev).reshape(-1) for a in axes]
         if len(ax) != dim:
             raise ValueError("one axis per dimension of cov_samples")
-        from .summator import summate_grid
-
-        if prec == "mixed" and dim in (2, 3):
-            grid = summate_grid(cov, z1, z2, ax, precision="mixed", method="tensor",
-                                out_dtype="float64").reshape(-1)
-        else:
-            grid = summate_grid(cov, z1, z2, ax, precision=prec,
-                                method="pointwise").reshape(-1)
         x = (torch.empty((dim, 0), dtype=torch.float64, device=dev) if pos is None
              else _dev_f64(pos, dev).reshape(dim, -1))
-        out = grid
+        n_grid = 1
+        for a in ax:
+            n_grid *= a.numel()
+        # the grid's values, then the points', written in place
+        out = torch.empty(n_grid + x.shape[1], dtype=torch.float64, device=dev)
+        stream = _stream(dev)
+        lens = (ctypes.c_int64 * 4)(*([a.numel() for a in ax] + [1] * (4 - dim)))
+        flat = torch.cat(ax)
+        if prec == "mixed" and dim in (2, 3):
+            _native.call("gst_summate_grid_tc", dim, n_modes, lens, _p(flat), _p(cov),
+                         _p(z1), _p(z2), _p(out), _native.GST_OUT_F64, 1.0, stream)
+        elif prec == "mixed":
+            _native.call("gst_summate_grid_mixed", dim, n_modes, lens, _p(flat),
+                         _p(cov), _p(z1), _p(z2), _p(out), _native.GST_OUT_F64, 1.0,
+                         stream)
+        else:
+            _native.call("gst_summate_grid_f64", dim, n_modes, lens, _p(flat),
+                         _p(cov), _p(z1), _p(z2), _p(out), stream)
         if x.shape[1] > 0:
-            out = torch.empty(grid.numel() + x.shape[1], dtype=torch.float64,
-                              device=dev)
-            out[:grid.numel()] = grid
             name = "gst_summate_f64" if prec == "f64" else "gst_summate_mixed"
             args = [dim, n_modes, x.shape[1], _p(cov), _p(z1), _p(z2), _p(x),
-                    _p(out[grid.numel():])]
+                    _p(out[n_grid:])]
             if prec == "mixed":
                 args.append(_native.GST_OUT_F64)
-            _native.call(name, *args, _stream(dev))
+            _native.call(name, *args, stream)
         ctx.save_for_backward(cov, z1, z2, x, *ax)
         ctx.prec = prec
         ctx.in_devices = [t.device for t in (cov_samples, z_1, z_2)] + [
