@@ -354,8 +354,9 @@ class _ModeMapDevice(torch.autograd.Function):
         mt = torch.empty((dim, dim), dtype=torch.float64, device=prm.device)
         jac = torch.empty((dim * dim, prm.numel()), dtype=torch.float64,
                           device=prm.device)
-        _native.call("gst_mode_map", dim, _p(prm), float(len_scale_ref), _p(mt),
-                     _p(jac), _stream(prm.device))
+        with torch.cuda.device(prm.device):
+            _native.call("gst_mode_map", dim, _p(prm), float(len_scale_ref), _p(mt),
+                         _p(jac), _stream(prm.device))
         ctx.save_for_backward(jac)
         return mt
 
