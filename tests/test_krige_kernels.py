@@ -142,12 +142,14 @@ def _gauss_kriging_system(rng, k, n, dim=2, ls=3.0, nugget=1e-6):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["random", "kriging"])
-def test_sliced_variance_matches_oracle(cuda_lib, kind):
+@pytest.mark.parametrize("kind,n", [("random", 4096), ("kriging", 4096),
+                                    ("random", 4003)])
+def test_sliced_variance_matches_oracle(cuda_lib, kind, n):
     """Large K^2 n variances run as FP16 tensor-core products of error-free
-    FP64 slices: same scale-aware FP64 bar against the oracle."""
-    rng = np.random.RandomState(17 if kind == "random" else 18)
-    k, n = 1001, 4096
+    FP64 slices: same scale-aware FP64 bar against the oracle (K = 1001 and
+    n = 4003 exercise the zero padding of both GEMM dimensions)."""
+    rng = np.random.RandomState((17 if kind == "random" else 18) + n)
+    k = 1001
     if kind == "random":
         a = rng.normal(size=(k, k))
         mat = a @ a.T / k + np.eye(k)
